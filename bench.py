@@ -1,0 +1,423 @@
+"""Benchmark of the projection path on one GB300 (or N replicas under torchrun).
+
+Workload: the dense projector pair of the projector microbench -- N=2048
+image, 2048 angles in [0, pi), 2897 detectors, deltarho 1 -- on a seeded
+random-ellipse phantom (forward projection) and a U[0,1) sinogram
+(backprojection).  One step = one A*x (forward projection) plus one A^T*y
+(backprojection) through the library's C ABI.
+
+value: FP/BP GB/s = compulsory bytes of the step (image and sinogram read and
+written, 8*(N^2 + a*D)) / device time, inputs resident in HBM, L2 flushed
+before every step.  e2e: the same metric through the public drop-in API
+(futhark.forwardprojection / futhark.backprojection) from pinned host arrays,
+host<->device copies inside the timed region.
+
+--impl reference times the reference's CPU path (the FP32 C restatement of
+the Futhark programs, oracle/cpu_ref.c, every host core) on the same
+workload: a bounded sample of angles, scaled to the full angle count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+N_SIZE, N_ANGLES, N_DET = 2048, 2048, 2897
+METRIC = "SIRT ms to rel. residual 1e-3: warm-start vs plain, 1 GB300; FP/BP GB/s"
+WORKLOAD = "projector microbench, dense on-the-fly: N=2048 image, 2048 angles in [0,pi), 2897 detectors, deltarho=1"
+
+
+def step_bytes(N=N_SIZE, a=N_ANGLES, D=N_DET):
+    return 8 * (N * N + a * D)
+
+
+def flops_fp(N=N_SIZE, a=N_ANGLES, D=N_DET):
+    # 14 flops per ray-row step (forwardprojection.fut:32-56; FMA=2, add/mul/div=1)
+    return 14.0 * a * D * N
+
+
+def flops_bp(N=N_SIZE, a=N_ANGLES, rpp=2):
+    # 13 flops per (pixel, line) + 13 per ray evaluation (backprojection.fut:49-64)
+    return (13.0 + 13.0 * rpp) * N * N * a
+
+
+def workload(seed=0):
+    from synkrotomo_gb300 import phantom
+    g = phantom.geometry(N_SIZE, N_ANGLES, numrhos=N_DET)
+    img = phantom.ellipse_phantom(N_SIZE, seed)
+    sino = np.random.default_rng(seed + 1).random(N_ANGLES * N_DET).astype(np.float32)
+    return g, img, sino
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+# ---------------------------------------------------------------------------
+# CPU leg (oracle/cpu_ref.c: test infrastructure, used here only as the timed
+# stand-in for the reference's CPU build)
+# ---------------------------------------------------------------------------
+
+def cpu_reference_rate(budget_s=12.0, seed=0):
+    """Seconds per full FP+BP step of the workload on all host cores,
+    extrapolated from a sample of angles (both projectors are linear in the
+    angle count)."""
+    from oracle import cpu_ref
+    cores = host_cores()
+    cpu_ref.set_threads(cores)
+    g, img, sino = workload(seed)
+    D = N_DET
+
+    def run(na):
+        idx = np.linspace(0, N_ANGLES - 1, na).astype(int)
+        ang = g.angles[idx].copy()
+        sub = sino.reshape(N_ANGLES, D)[idx].ravel().copy()
+        t0 = time.perf_counter()
+        cpu_ref.forwardprojection(ang, g.rhozero, g.deltarho, D, img)
+        t1 = time.perf_counter()
+        cpu_ref.backprojection(ang, g.rhozero, g.deltarho, N_SIZE, sub)
+        t2 = time.perf_counter()
+        return t1 - t0, t2 - t1
+
+    na = 4
+    fpt, bpt = run(na)
+    per_angle = (fpt + bpt) / na
+    na2 = int(max(4, min(N_ANGLES, (budget_s * 0.8) / max(per_angle, 1e-6))))
+    if na2 > na:
+        fpt, bpt = run(na2)
+        na = na2
+    scale = N_ANGLES / na
+    return {"fp_s": fpt * scale, "bp_s": bpt * scale, "step_s": (fpt + bpt) * scale, "sample_angles": na,
+            "cores": cores}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu_index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def ncu_traffic(name):
+    """Per-launch DRAM bytes of a kernel from its committed ncu summary
+    (profiles/<name>.md, line 'traffic_bytes_per_launch: X'), else None."""
+    path = os.path.join(ROOT, "profiles", f"{name}.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].strip().split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    from synkrotomo_gb300 import runtime as rt
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g, img, sino = workload(seed=rank)
+    ang_d = torch.from_numpy(g.angles).to(dev)
+    img_d = torch.from_numpy(img).to(dev)
+    sino_d = torch.from_numpy(sino).to(dev)
+    fp_out = torch.empty(N_ANGLES * N_DET, device=dev)
+    bp_out = torch.empty(N_SIZE * N_SIZE, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # 512 MB > 129 MB L2
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        rt.forwardprojection(ang_d, g.rhozero, g.deltarho, N_DET, img_d, out=fp_out)
+        rt.backprojection(ang_d, g.rhozero, g.deltarho, N_SIZE, sino_d, out=bp_out)
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(dev.index) as clk:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))         # L2 flush outside the timed events
+            e0, e1, e2 = ev[i]
+            e0.record(stream)
+            rt.forwardprojection(ang_d, g.rhozero, g.deltarho, N_DET, img_d, out=fp_out)
+            e1.record(stream)
+            rt.backprojection(ang_d, g.rhozero, g.deltarho, N_SIZE, sino_d, out=bp_out)
+            e2.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    rt.context(dev.index).sync()
+    fp_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    bp_ms = [b.elapsed_time(c) for _, b, c in ev]
+    step_ms = sum(fp_ms) / len(fp_ms) + sum(bp_ms) / len(bp_ms)
+    if world > 1:
+        t = torch.tensor([step_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+        torch.distributed.barrier()
+
+    # end to end through the public API, pinned host buffers
+    e2e = run_e2e(args, g, img, sino, dev)
+    sirt = run_sirt_cfg0(dev) if (rank == 0 and not args.skip_sirt) else None
+    return {"step_ms": step_ms, "fp_ms": statistics.median(fp_ms), "bp_ms": statistics.median(bp_ms),
+            "wall_s": wall, "clocks": clk.summary(), "e2e": e2e, "sirt": sirt,
+            "sms": torch.cuda.get_device_properties(dev).multi_processor_count}
+
+
+def run_e2e(args, g, img, sino, dev):
+    import torch
+
+    from futhark import backprojection, forwardprojection
+
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float32, pin_memory=True)
+        t.numpy()[:] = a
+        return t.numpy()
+
+    ang_h, img_h, sino_h = pinned(g.angles), pinned(img), pinned(sino)
+    fpm, bpm = forwardprojection.forwardprojection(), backprojection.backprojection()
+
+    def step():
+        s = fpm.main(ang_h, g.rhozero, g.deltarho, N_DET, img_h).get()
+        b = bpm.main(ang_h, g.rhozero, g.deltarho, N_SIZE, sino_h).get()
+        return s, b
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    h2d = 4 * (2 * N_ANGLES + N_SIZE * N_SIZE + N_ANGLES * N_DET)
+    d2h = 4 * (N_ANGLES * N_DET + N_SIZE * N_SIZE)
+    return {"ms": ms, "h2d": h2d, "d2h": d2h}
+
+
+def run_sirt_cfg0(dev):
+    """Plain SIRT on the reference's CPU-runnable configuration (N=128, 128
+    angles, 182 detectors, 1 % noise): ms for 200 iterations, and ms to the
+    relative residual that 200 plain iterations reach."""
+    import torch
+
+    from synkrotomo_gb300 import phantom
+    from synkrotomo_gb300 import runtime as rt
+
+    g = phantom.geometry(128, 128)
+    img = torch.from_numpy(phantom.ellipse_phantom(128, 0)).to(dev)
+    ang = torch.from_numpy(g.angles).to(dev)
+    b = rt.forwardprojection(ang, g.rhozero, g.deltarho, g.numrhos, img).cpu().numpy()
+    b = torch.from_numpy(phantom.add_noise(b, 0, 0.01)).to(dev)
+    x0 = torch.zeros(128 * 128, device=dev)
+    _, res, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, 128, 1, x0, b, 200, residuals=True)
+    target = float(res[0, 200].item()) * 1.01
+    out = {}
+    for label, tol in (("200_iterations", 0.0), ("to_residual", target)):
+        for _ in range(3):
+            rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, 128, 1, x0, b, 200, tol=tol)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _, _, done = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, 128, 1, x0, b, 200, tol=tol)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        out[label] = {"ms": statistics.median(ts), "iterations": int(done.item())}
+    out["target_residual"] = target
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-sirt", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        r = None
+        times = []
+        for _ in range(args.warmup + args.steps):
+            r = cpu_reference_rate(budget_s=8.0)
+            times.append(r["step_s"])
+        step_s = statistics.median(times[args.warmup:])
+        value = step_bytes() / step_s / 1e9
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "l2": "n/a (host CPU)"},
+                "cpu_baseline": {"value": value, "unit": "GB/s", "cores": r["cores"], "kind": "port",
+                                 "sample": f"{r['sample_angles']} of {N_ANGLES} angles per step, scaled x"
+                                           f"{N_ANGLES / r['sample_angles']:.1f} (oracle/cpu_ref.c, "
+                                           f"{cpu_model()})"},
+                "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    if world > 1:
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from synkrotomo_gb300 import _lib
+    _lib.load()
+
+    res = run_gpu(args, rank, world)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return 0
+
+    value = world * step_bytes() / (res["step_ms"] * 1e-3) / 1e9
+    peaks = measured_peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = res["sms"] * 128 * 2 * sm_max * 1e6 / 1e12     # TFLOP/s
+    fp_tf = flops_fp() / (res["fp_ms"] * 1e-3) / 1e12
+    bp_tf = flops_bp() / (res["bp_ms"] * 1e-3) / 1e12
+    dom = "bp" if res["bp_ms"] >= res["fp_ms"] else "fp"
+    achieved = bp_tf if dom == "bp" else fp_tf
+    kname = "bp_kernel_dense2048" if dom == "bp" else "fp_kernel_dense2048"
+    roofline = {"bound": "fp32", "kernel": "bp_kernel" if dom == "bp" else "fp_kernel", "achieved": achieved,
+                "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                "traffic": ncu_traffic(kname),
+                "peak_source": f"nominal FP32: {res['sms']} SMs x 128 FMA/clk x 2 x {sm_max:.0f} MHz "
+                               "(MEASURED_PEAKS.json has no FP32 figure)",
+                "fp_tflops": fp_tf, "bp_tflops": bp_tf}
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["step_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "image": N_SIZE, "angles": N_ANGLES, "detectors": N_DET,
+                       "step": "forward projection + backprojection", "l2": "flushed (512 MB write) before every step",
+                       "parallelism": f"replicas x{world}"},
+            "fp_ms": res["fp_ms"], "bp_ms": res["bp_ms"],
+            "gpu_launches": 5 * args.steps,
+            "clocks": res["clocks"], "roofline": roofline}
+    e = res["e2e"]
+    line["e2e"] = {"value": world * step_bytes() / (e["ms"] * 1e-3) / 1e9, "unit": "GB/s",
+                   "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["ms"]}
+    if res["sirt"] is not None:
+        line["sirt_cfg0"] = res["sirt"]
+    if not args.skip_cpu:
+        r = cpu_reference_rate(budget_s=10.0)
+        cv = step_bytes() / r["step_s"] / 1e9
+        line["cpu_baseline"] = {"value": cv, "unit": "GB/s", "cores": r["cores"], "kind": "port",
+                                "sample": f"{r['sample_angles']} of {N_ANGLES} angles, scaled to all angles "
+                                          f"(oracle/cpu_ref.c, {cpu_model()})"}
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

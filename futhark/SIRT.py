@@ -1,0 +1,7 @@
+"""Drop-in for the reference module `futhark.SIRT` (program futhark/SIRT.fut:43-49).
+
+Usage as in the reference: ``SIRT.SIRT().main(...).get()``.
+"""
+from synkrotomo_gb300.dropin import SIRT
+
+__all__ = ["SIRT"]

@@ -1,0 +1,132 @@
+/*
+ * libsynk: GB300-native (sm_103a) parallel-beam projection and SIRT.
+ *
+ * C ABI of the drop-in boundary.  The reference (tomograph/synkrotomo) is a
+ * set of Futhark programs whose entry point `main` is exposed by Futhark's
+ * generated libraries: `futhark pyopencl --library` (Makefile:1-4, the Python
+ * classes of README.md:21-25) and `futhark c --library` (Makefile:6-9), whose
+ * C API is a context object (futhark_context_new / _sync / _get_error /
+ * _free) plus one `futhark_entry_main(ctx, &out, in0, in1, ...)` per program.
+ * This header keeps that shape: one context per device and stream, one entry
+ * point per reference program with the program's own argument order, the
+ * output first, an int status (0 = success), errors described by
+ * synk_context_get_error().
+ *
+ * Conventions:
+ *  - Every array argument is a DEVICE pointer to contiguous float32 data of
+ *    the stated length; lengths are element counts.  Scalars follow the
+ *    reference's f32 / i32 types.
+ *  - Entry points are stream-ordered: they enqueue work on the context's
+ *    stream and return launch/validation errors.  Errors that happen while
+ *    the GPU runs (a persistent kernel's grid barrier that timed out) are
+ *    reported by the next synk_context_sync().
+ *  - Inputs are never modified.  Scratch memory is taken from CUDA's
+ *    stream-ordered allocator (cudaMallocAsync) on the context's stream.
+ *  - A context is used by one host thread at a time.
+ *  - Geometry: ray (angle theta, detector r) is the line
+ *    rho = x*cos(theta) - y*sin(theta), rho = rhozero + r*deltarho,
+ *    x = col - size/2, y = row - size/2 (futhark/forwardprojection.fut:26-29).
+ *    Images are row-major [size*size]; sinograms angle-major [a*numrhos].
+ */
+#ifndef SYNK_H
+#define SYNK_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SYNK_OK 0
+#define SYNK_EINVAL 1    /* bad argument (shape, size, null pointer)       */
+#define SYNK_ECUDA 2     /* a CUDA runtime call failed                     */
+#define SYNK_ETIMEOUT 3  /* a persistent kernel's grid barrier timed out   */
+#define SYNK_ENOMEM 4    /* device allocation failed                       */
+
+typedef struct synk_context synk_context;
+
+/* ---- context (futhark_context_new / _free / _sync / _get_error) ---- */
+
+/* Creates a context on CUDA device `device` that enqueues on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream). */
+int synk_context_new(synk_context **out, int device, void *stream);
+void synk_context_free(synk_context *ctx);
+/* Redirects subsequent work to another stream of the same device. */
+int synk_context_set_stream(synk_context *ctx, void *stream);
+/* Waits for the context's stream; returns SYNK_ETIMEOUT if a persistent
+ * kernel gave up at a grid barrier, SYNK_ECUDA on an asynchronous CUDA error. */
+int synk_context_sync(synk_context *ctx);
+/* Message of the last failure on this context ("" when none).  The pointer
+ * stays valid until the next call on the context. */
+const char *synk_context_get_error(synk_context *ctx);
+/* Library version string. */
+const char *synk_version(void);
+
+/* ---- entry points of the reference programs ---- */
+
+/* futhark/forwardprojection.fut:71-84 `main (angles, rhozero, deltarho,
+ * numrhos, image)`: out[a*numrhos] = angle-major sinogram of the
+ * size x size image, size = sqrt(n). */
+int synk_forwardprojection(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
+                           float deltarho, int32_t numrhos, const float *image, int64_t n);
+
+/* futhark/forwardprojection_sparse.fut:26-40: the same program, benchmarked by
+ * the reference on sparse-view (1..95 angle) datasets. */
+int synk_forwardprojection_sparse(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
+                                  float deltarho, int32_t numrhos, const float *image, int64_t n);
+
+/* futhark/backprojection.fut:82-93 `main (angles, rhozero, deltarho, size,
+ * projections)`: out[size*size] = backprojection of projections[p],
+ * numrhos = p / a. */
+int synk_backprojection(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
+                        float deltarho, int32_t size, const float *projections, int64_t p);
+
+/* futhark/backprojection_sparse.fut:26-37: same program, sparse-view datasets. */
+int synk_backprojection_sparse(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
+                               float deltarho, int32_t size, const float *projections, int64_t p);
+
+/* futhark/SIRT.fut:43-49 `main (angles, rhozero, deltarho, image,
+ * projections, iterations)`: out[n] = `iterations` SIRT updates
+ * x <- x + C*BP(R*(b - FP(x))) starting from image[n] (SIRT.fut:9-41). */
+int synk_SIRT(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero, float deltarho,
+              const float *image, int64_t n, const float *projections, int64_t p, int32_t iterations);
+
+/* futhark/SIRT3D.fut:18-29 `main (angles, rhos, projections, iterations,
+ * size)`: `size` independent slices (zero start), slice i reconstructed from
+ * projections[i*r*a : (i+1)*r*a]; out[size*size*size].  rhozero = rhos[0],
+ * deltarho = rhos[1] - rhos[0] (the convention of
+ * archive/projection_lib.fut:114-115; the reference's own call passes rhos
+ * where SIRT expects those two scalars). */
+int synk_SIRT3D(synk_context *ctx, float *out, const float *angles, int64_t a, const float *rhos, int64_t r,
+                const float *projections, int64_t p, int32_t iterations, int32_t size);
+
+/* ---- extended SIRT (no reference counterpart: stopping rule, history) ---- */
+
+typedef struct synk_sirt_options {
+    /* Stop once ||FP(x_k) - b|| / ||b|| <= tol (0 = run all iterations).  The
+     * residual of x_k is measured in the forward pass of iteration k. */
+    double tol;
+    /* Optional DEVICE array [iterations+1] (per slice: [nslices][iterations+1])
+     * receiving ||FP(x_k) - b|| / ||b|| for k = 0..iterations (entries after a
+     * stop stay as they were).  NULL = not recorded. */
+    double *residuals;
+    /* Optional DEVICE array [nslices] receiving the number of updates applied. */
+    int32_t *iterations_done;
+    /* Rows (FP) / angles (BP) split per work item: 0 = automatic. */
+    int32_t fp_split;
+    int32_t bp_split;
+} synk_sirt_options;
+
+/* SIRT of `nslices` independent slices sharing one geometry in ONE persistent
+ * launch: image/out/projections hold nslices consecutive slices ([nslices*n]
+ * and [nslices*p]); image may be NULL for a zero start. */
+int synk_sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
+                     float deltarho, int32_t numrhos, int32_t size, int32_t nslices, const float *image,
+                     const float *projections, int32_t iterations, const synk_sirt_options *opts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SYNK_H */

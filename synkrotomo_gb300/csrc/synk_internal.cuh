@@ -1,0 +1,283 @@
+// Internal device-side definitions shared by the projector, SIRT and CSR
+// kernels of libsynk.  Geometry convention (futhark/forwardprojection.fut:26-29,
+// futhark/sirtlib.fut:41): the ray of angle theta and detector r is the line
+// rho = x*cos(theta) - y*sin(theta), rho = rhozero + r*deltarho, with
+// x = col - N/2, y = row - N/2 and pixel (row, col) = [x, x+1) x [y, y+1).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/synk.h"
+
+namespace synk {
+
+// ---------------------------------------------------------------------------
+// Per-angle geometry table (48 bytes, read as three float4 by the kernels).
+// ---------------------------------------------------------------------------
+struct __align__(16) AngleGeom {
+    // Reference line triple in the traversal frame (sirtlib.fut:41): steep
+    // lines (cos, -sin, lsteep) on the image, flat lines (-sin, cos, lflat)
+    // on the transposed image.
+    float cost, sint, lbase, slope;   // slope = -sint/cost (forwardprojection.fut:26)
+    // Chord-length trapezoid in the true frame: for a pixel whose centre has
+    // rho_c, a ray at rho has length lbase * sat((h - |rho - rho_c|) / b) with
+    // a = max(|cos|,|sin|), b = min(|cos|,|sin|), h = (a+b)/2.
+    float c, s, h_over_b, inv_b;      // cos, sin, h/b, 1/b (both capped)
+    // Forward traversal constants and path selection.
+    float slope_lo;    // min(slope, 0): xlo = xbot + slope_lo
+    float ainv;        // 1/|slope| (capped)
+    int   flat;        // 1: the line traverses the transposed image
+    int   exact;       // 1: near-axis line, evaluate the reference's own formulas
+};
+static_assert(sizeof(AngleGeom) == 48, "AngleGeom layout");
+
+// |slope| below this uses the reference's own f32 expression order (see
+// geometry.cu): there a ray can run along a pixel edge for its whole length
+// and the rounding of the reference's expressions decides which column gets it.
+constexpr float kExactSlope = 1.0f / 4096.0f;
+constexpr float kCap = 1.0e30f;
+
+// sqrt(2)/2 evaluated as the reference does in f32 (backprojection.fut:20).
+__host__ __device__ inline float fact_f32() { return 0.70710677f; }
+
+// ---------------------------------------------------------------------------
+// Floor without the conversion unit (Blackwell's F2I/FRND issue at a quarter
+// of the FP32 rate).  Adding 1.5*2^23 with round-toward-minus-infinity leaves
+// floor(x) in the low mantissa bits for |x| < 2^22 (the classic "magic number"
+// rounding of IEEE-754 single precision): two FP32 adds and an integer add.
+// ---------------------------------------------------------------------------
+constexpr float kMagic = 12582912.0f;     // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+
+__device__ __forceinline__ float floor_magic(float x, int &ix) {
+    const float r = __fadd_rd(x, kMagic);
+    ix = __float_as_int(r) - kMagicBits;
+    return __fsub_rn(r, kMagic);
+}
+__device__ __forceinline__ float ceil_magic(float x, int &ix) {
+    const float r = __fadd_ru(x, kMagic);
+    ix = __float_as_int(r) - kMagicBits;
+    return __fsub_rn(r, kMagic);
+}
+
+// Neumaier-compensated accumulation of a block partial into (sum, comp).
+__device__ __forceinline__ void comp_add(float &sum, float &comp, float v) {
+    const float t = __fadd_rn(sum, v);
+    if (fabsf(sum) >= fabsf(v)) comp = __fadd_rn(comp, __fadd_rn(__fsub_rn(sum, t), v));
+    else comp = __fadd_rn(comp, __fadd_rn(__fsub_rn(v, t), sum));
+    sum = t;
+}
+
+// ---------------------------------------------------------------------------
+// One 2D problem as the kernels see it.
+// ---------------------------------------------------------------------------
+struct ProbGeom {
+    int N;          // image is N x N (N even)
+    int half;       // N/2
+    int a;          // angles
+    int D;          // detectors per angle (numrhos)
+    int rpp;        // rhos per pixel: ceil(sqrt(2)/deltarho) (backprojection.fut:87)
+    float rhozero;
+    float deltarho;
+    float inv_deltarho;
+    const AngleGeom *geom;   // [a]
+};
+
+// ---------------------------------------------------------------------------
+// Forward projection of one ray: sum over the rows of the traversal frame.
+// img points at the image seen in that frame (the transposed image for flat
+// lines).  ONES replaces every in-bounds pixel by 1 (normaliser R, FP64 sum).
+// ---------------------------------------------------------------------------
+template <bool ONES>
+struct FpAcc;
+template <> struct FpAcc<false> { typedef float T; };
+template <> struct FpAcc<true> { typedef double T; };
+
+// Rows [j0, j1) of the fast path, accumulated into (sum, comp): partial sums
+// over 32 rows, compensated across partials.
+template <bool ONES>
+__device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int N, float slope, float u0,
+                                             float ainv, int j0, int j1,
+                                             typename FpAcc<ONES>::T &sum, float &comp) {
+    const float bias = 1.0f - ainv;
+    const unsigned uN = (unsigned)N;
+    int j = j0;
+    while (j < j1) {
+        const int jend = min(j + 32, j1);
+        float part = 0.0f;
+        const float *row = img + (size_t)j * N;
+#pragma unroll 4
+        for (; j < jend; ++j, row += N) {
+            // u = left end of the row segment in pixel-index coordinates
+            const float u = fmaf((float)j, slope, u0);
+            int c;
+            const float fl = floor_magic(u, c);
+            const float t = fmaxf(fmaf(__fsub_rn(u, fl), ainv, bias), 0.0f);  // share of pixel c+1
+            float v0, v1;
+            if constexpr (ONES) {
+                v0 = ((unsigned)c < uN) ? 1.0f : 0.0f;
+                v1 = ((unsigned)(c + 1) < uN) ? 1.0f : 0.0f;
+            } else {
+                v0 = ((unsigned)c < uN) ? __ldg(row + c) : 0.0f;
+                v1 = ((unsigned)(c + 1) < uN) ? __ldg(row + c + 1) : 0.0f;
+            }
+            part += fmaf(t, v1 - v0, v0);
+        }
+        if constexpr (ONES) sum += (double)part;
+        else comp_add(sum, comp, part);
+    }
+}
+
+// The reference's own expressions (forwardprojection.fut:31-56), used for
+// near-axis lines: every operation rounds exactly as the f32 reference.
+template <bool ONES>
+__device__ __forceinline__ void fp_rows_exact(const float *__restrict__ img, int N, int half, float slope,
+                                              float intercept, float lbase,
+                                              typename FpAcc<ONES>::T &sum) {
+    const int size = N;
+    typename FpAcc<ONES>::T acc = 0;
+    for (int i = -half; i < half; ++i) {
+        const float xbot = __fadd_rn(__fmul_rn((float)i, slope), intercept);
+        const float xtop = __fadd_rn(xbot, slope);
+        const int xpb = (int)floorf(xbot);
+        const int xpt = (int)floorf(xtop);
+        const float xpmax = (float)max(xpb, xpt);
+        const float xdiff = __fsub_rn(xtop, xbot);
+        const bool single = xpb == xpt;
+        const bool botin = xpb >= -half && xpb < half;
+        const bool topin = (!single) && xpt >= -half && xpt < half;
+        const float lxbot = single ? lbase : __fmul_rn(__fdiv_rn(__fsub_rn(xpmax, xbot), xdiff), lbase);
+        const float lxtop = __fmul_rn(__fdiv_rn(__fsub_rn(xtop, xpmax), xdiff), lbase);
+        const float *row = ONES ? nullptr : img + (size_t)(i + half) * size + half;
+        float bot = 0.0f, top = 0.0f;
+        if constexpr (ONES) {
+            if (botin) bot = lxbot;
+            if (topin) top = lxtop;
+        } else {
+            if (botin) bot = __fmul_rn(lxbot, __ldg(row + xpb));
+            if (topin) top = __fmul_rn(lxtop, __ldg(row + xpt));
+        }
+        acc += ONES ? (typename FpAcc<ONES>::T)((double)bot + (double)top)
+                    : (typename FpAcc<ONES>::T)__fadd_rn(bot, top);
+    }
+    sum = acc;
+}
+
+// Ray sum of detector r of the angle with geometry g.  Returns the reference
+// value sum_rows(lbot*img[bot] + ltop*img[top]) (lbase already applied).
+template <bool ONES>
+__device__ __forceinline__ typename FpAcc<ONES>::T fp_ray(const ProbGeom &P, const AngleGeom &g,
+                                                          const float *__restrict__ img_frame, int r,
+                                                          int jbeg, int jend) {
+    typedef typename FpAcc<ONES>::T T;
+    const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));   // forwardprojection.fut:28
+    const float intercept = __fdiv_rn(rho, g.cost);                               // forwardprojection.fut:29
+    // |rho| of any point of the image is at most N/sqrt(2): such a ray adds nothing
+    if (fabsf(rho) > 0.75f * (float)P.N + 2.0f) return (T)0;
+    if (g.exact) {
+        // whole ray in one piece (only the row-part starting at 0 computes it)
+        if (jbeg != 0) return (T)0;
+        T s;
+        fp_rows_exact<ONES>(img_frame, P.N, P.half, g.slope, intercept, g.lbase, s);
+        return s;
+    }
+    // u(j) = xlo(row j) + half, xlo = xbot + min(slope,0), xbot = (j-half)*slope + intercept
+    const float halff = (float)P.half;
+    const float u0 = intercept + g.slope_lo + halff - halff * g.slope;
+    // rows where the segment [u, u+|slope|] can touch a pixel column in [0, N)
+    const float aslope = fabsf(g.slope);
+    int j0 = jbeg, j1 = jend;
+    if (g.slope != 0.0f) {
+        const float ja = (-1.0f - aslope - u0) / g.slope;
+        const float jb = ((float)P.N - u0) / g.slope;
+        float lo = fminf(ja, jb), hi = fmaxf(ja, jb);
+        lo = fmaxf(lo - 1.0f, (float)jbeg);
+        hi = fminf(hi + 2.0f, (float)jend);
+        j0 = (int)lo;
+        j1 = (hi > lo) ? (int)hi : j0;
+    } else if (!(u0 > -1.0f && u0 < (float)P.N)) {
+        j1 = j0;
+    }
+    T sum = (T)0;
+    float comp = 0.0f;
+    fp_rows_fast<ONES>(img_frame, P.N, g.slope, u0, g.ainv, j0, j1, sum, comp);
+    if (ONES) return sum * (double)g.lbase;
+    return (T)(((float)sum + comp) * g.lbase);
+}
+
+// ---------------------------------------------------------------------------
+// Backprojection of one pixel for one angle: sum over the candidate
+// detectors.  Returns the contribution with lbase applied.
+// ---------------------------------------------------------------------------
+template <bool ONES>
+__device__ __forceinline__ float bp_angle(const ProbGeom &P, const AngleGeom &g, const float *__restrict__ sino_row,
+                                          int row, int col) {
+    const int half = P.half;
+    const int D = P.D;
+    if (!g.exact) {
+        const float xc = (float)(col - half) + 0.5f;
+        const float yc = (float)(row - half) + 0.5f;
+        const float rhoc = fmaf(xc, g.c, -yc * g.s);
+        int s0;
+        ceil_magic((rhoc - fact_f32() - P.rhozero) * P.inv_deltarho, s0);
+        float acc = 0.0f;
+        float d = fmaf((float)s0, P.deltarho, P.rhozero) - rhoc;
+        for (int q = 0; q < P.rpp; ++q, d += P.deltarho) {
+            const int det = s0 + q;
+            const float w = __saturatef(fmaf(-fabsf(d), g.inv_b, g.h_over_b));
+            if ((unsigned)det < (unsigned)D) acc = fmaf(w, ONES ? 1.0f : __ldg(sino_row + det), acc);
+        }
+        return acc * g.lbase;
+    }
+    // Near-axis line: the reference's own f32 expressions (backprojection.fut:46-64)
+    // in the line's frame (flat lines see the transposed image, 75-77).
+    const float xmin = (float)(g.flat ? row - half : col - half);
+    const float ymin = (float)(g.flat ? col - half : row - half);
+    const float fact = fact_f32();
+    const float cost = g.cost, sint = g.sint;
+    const float x = __fsub_rn(__fadd_rn(xmin, 0.5f), __fmul_rn(fact, cost));
+    const float y = __fsub_rn(__fadd_rn(ymin, 0.5f), __fmul_rn(fact, sint));
+    const float rho = __fadd_rn(__fmul_rn(cost, x), __fmul_rn(sint, y));
+    const float s = ceilf(__fdiv_rn(__fsub_rn(rho, P.rhozero), P.deltarho));
+    const float xbase = __fmul_rn(ymin, g.slope);
+    float acc = 0.0f;
+    for (int i = 0; i < P.rpp; ++i) {
+        const float sprime = __fadd_rn(s, (float)i);
+        const float r = __fadd_rn(__fmul_rn(sprime, P.deltarho), P.rhozero);
+        const float xbot = __fadd_rn(xbase, __fdiv_rn(r, cost));
+        const float xtop = __fadd_rn(xbot, g.slope);
+        const float maxx = fmaxf(xbot, xtop), minx = fminf(xbot, xtop);
+        // intersect_fact (backprojection.fut:22-33)
+        const float lo = fmaxf(__fsub_rn(maxx, xmin), 0.0f);
+        const float hi = fmaxf(__fsub_rn(__fadd_rn(xmin, 1.0f), minx), 0.0f);
+        const float diff = __fsub_rn(maxx, minx);
+        const float inside = fminf(lo, hi);
+        const float prop = inside == 0.0f ? 0.0f : __fdiv_rn(inside, diff);
+        const float l = __fmul_rn(fminf(prop, 1.0f), g.lbase);
+        const int det = (int)sprime;
+        if (det >= 0 && det < D) acc = __fadd_rn(acc, __fmul_rn(l, ONES ? 1.0f : __ldg(sino_row + det)));
+    }
+    return acc;
+}
+
+__device__ __forceinline__ AngleGeom load_geom(const AngleGeom *__restrict__ gt, int k) {
+    const float4 *p = reinterpret_cast<const float4 *>(gt + k);
+    const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    AngleGeom g;
+    g.cost = a.x; g.sint = a.y; g.lbase = a.z; g.slope = a.w;
+    g.c = b.x; g.s = b.y; g.h_over_b = b.z; g.inv_b = b.w;
+    g.slope_lo = c.x; g.ainv = c.y; g.flat = __float_as_int(c.z); g.exact = __float_as_int(c.w);
+    return g;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel launchers implemented in the .cu files (all enqueue on `stream`).
+// ---------------------------------------------------------------------------
+cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStream_t stream);
+cudaError_t launch_transpose(const float *in, float *out, int N, int nslices, cudaStream_t stream);
+cudaError_t launch_fp(const ProbGeom &P, const float *img, const float *imgT, float *sino, cudaStream_t stream);
+cudaError_t launch_bp(const ProbGeom &P, const float *sino, float *img, cudaStream_t stream);
+cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, cudaStream_t stream);
+
+}  // namespace synk

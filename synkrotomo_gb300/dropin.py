@@ -1,0 +1,116 @@
+"""Classes behind the ``futhark`` drop-in package.
+
+The reference's Python surface is generated by ``futhark pyopencl --library``
+(Makefile:1-4): one module per program, one class named after the module,
+an ``entry_points`` table and a ``main(*args)`` method returning a device
+array that callers ``.get()`` (README.md:21-25).  These classes keep those
+names, the argument order, the float32 / int32 argument types and the
+flattened layouts, and run on libsynk instead of OpenCL.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import runtime as rt
+
+
+class _Entry:
+    """Common constructor: the reference's keyword arguments (OpenCL platform
+    and device preferences, group sizes) are accepted and ignored; ``device``
+    selects the CUDA device."""
+
+    entry_points: dict = {}
+
+    def __init__(self, *args, device: int | None = None, **kwargs):
+        if not torch.cuda.is_available():
+            raise RuntimeError(f"{type(self).__name__}: a CUDA GPU is required (no CPU fallback exists)")
+        self.device = torch.cuda.current_device() if device is None else int(device)
+        rt.context(self.device)   # loads libsynk now: fail at construction, not at first call
+
+    def _wrap(self, t: torch.Tensor) -> rt.DeviceArray:
+        return rt.DeviceArray(t, rt.context(self.device))
+
+
+class forwardprojection(_Entry):
+    """futhark/forwardprojection.fut:71-84."""
+
+    entry_points = {"main": (["[]f32", "f32", "f32", "i32", "[]f32"], ["[]f32"])}
+    _sparse = False
+
+    def main(self, angles, rhozero, deltarho, numrhos, image):
+        with torch.cuda.device(self.device):
+            a = rt.to_device_f32(angles, 0, "angles", self.device)
+            rz = rt.scalar_f32(rhozero, 1, "rhozero")
+            dr = rt.scalar_f32(deltarho, 2, "deltarho")
+            nr = rt.scalar_i32(numrhos, 3, "numrhos")
+            img = rt.to_device_f32(image, 4, "image", self.device)
+            out = rt.forwardprojection(a, rz, dr, nr, img, sparse=self._sparse)
+            return self._wrap(out)
+
+
+class forwardprojection_sparse(forwardprojection):
+    """futhark/forwardprojection_sparse.fut:26-40 (same program, sparse-view data)."""
+
+    _sparse = True
+
+
+class backprojection(_Entry):
+    """futhark/backprojection.fut:82-93."""
+
+    entry_points = {"main": (["[]f32", "f32", "f32", "i32", "[]f32"], ["[]f32"])}
+    _sparse = False
+
+    def main(self, angles, rhozero, deltarho, size, projections):
+        with torch.cuda.device(self.device):
+            a = rt.to_device_f32(angles, 0, "angles", self.device)
+            rz = rt.scalar_f32(rhozero, 1, "rhozero")
+            dr = rt.scalar_f32(deltarho, 2, "deltarho")
+            sz = rt.scalar_i32(size, 3, "size")
+            proj = rt.to_device_f32(projections, 4, "projections", self.device)
+            out = rt.backprojection(a, rz, dr, sz, proj, sparse=self._sparse)
+            return self._wrap(out)
+
+
+class backprojection_sparse(backprojection):
+    """futhark/backprojection_sparse.fut:26-37 (same program, sparse-view data)."""
+
+    _sparse = True
+
+
+class SIRT(_Entry):
+    """futhark/SIRT.fut:43-49."""
+
+    entry_points = {"main": (["[]f32", "f32", "f32", "*[]f32", "[]f32", "i32"], ["[]f32"])}
+
+    def main(self, angles, rhozero, deltarho, image, projections, iterations):
+        with torch.cuda.device(self.device):
+            a = rt.to_device_f32(angles, 0, "angles", self.device)
+            rz = rt.scalar_f32(rhozero, 1, "rhozero")
+            dr = rt.scalar_f32(deltarho, 2, "deltarho")
+            img = rt.to_device_f32(image, 3, "image", self.device)
+            proj = rt.to_device_f32(projections, 4, "projections", self.device)
+            its = rt.scalar_i32(iterations, 5, "iterations")
+            out = rt.sirt(a, rz, dr, img, proj, its)
+            return self._wrap(out)
+
+
+class SIRT3D(_Entry):
+    """futhark/SIRT3D.fut:18-29 (intended semantics: rhozero = rhos[0],
+    deltarho = rhos[1] - rhos[0], ``size`` slices from a zero start)."""
+
+    entry_points = {"main": (["[]f32", "[]f32", "[]f32", "i32", "i32"], ["[]f32"])}
+
+    def main(self, angles, rhos, projections, iterations, size):
+        with torch.cuda.device(self.device):
+            a = rt.to_device_f32(angles, 0, "angles", self.device)
+            rh = rt.to_device_f32(rhos, 1, "rhos", self.device)
+            proj = rt.to_device_f32(projections, 2, "projections", self.device)
+            its = rt.scalar_i32(iterations, 3, "iterations")
+            sz = rt.scalar_i32(size, 4, "size")
+            out = rt.sirt3d(a, rh, proj, its, sz)
+            return self._wrap(out)
+
+
+def _np(x):
+    return np.asarray(x)

@@ -1,0 +1,263 @@
+"""Host runtime over libsynk: contexts bound to torch's CUDA streams, argument
+conversion and checks in the reference's terms, and the device-array object
+returned by the drop-in entry points.
+
+PyTorch is used for device memory and streams only; every computation is a
+libsynk kernel.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+
+__all__ = [
+    "SynkError", "DeviceArray", "context", "to_device_f32", "forwardprojection", "backprojection", "sirt",
+    "sirt_slices", "sirt3d",
+]
+
+
+class SynkError(RuntimeError):
+    """A libsynk call failed; ``code`` is the SYNK_* status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+class _Context:
+    def __init__(self, device: int):
+        L = _lib.load()
+        h = ctypes.c_void_p()
+        rc = L.synk_context_new(ctypes.byref(h), int(device), None)
+        if rc != 0:
+            raise SynkError(rc, f"synk_context_new(device={device}) failed with status {rc}")
+        self.handle = h
+        self.device = int(device)
+        self.lib = L
+
+    def bind(self, stream: torch.cuda.Stream | None = None):
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        self.lib.synk_context_set_stream(self.handle, ctypes.c_void_p(st.cuda_stream))
+        return self
+
+    def check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.lib.synk_context_get_error(self.handle).decode()
+            if rc == _lib.SYNK_EINVAL:
+                raise ValueError(f"{what}: {msg}")
+            raise SynkError(rc, f"{what}: {msg}")
+
+    def sync(self):
+        rc = self.lib.synk_context_sync(self.handle)
+        self.check(rc, "synk_context_sync")
+
+
+_contexts: dict[int, _Context] = {}
+_ctx_lock = threading.Lock()
+
+
+def context(device: int | None = None) -> _Context:
+    """The libsynk context of ``device`` (default: torch's current device),
+    bound to torch's current stream on that device."""
+    if not torch.cuda.is_available():
+        raise RuntimeError("synkrotomo_gb300 needs a CUDA GPU (no CPU fallback exists)")
+    dev = torch.cuda.current_device() if device is None else int(device)
+    with _ctx_lock:
+        ctx = _contexts.get(dev)
+        if ctx is None:
+            ctx = _contexts[dev] = _Context(dev)
+    return ctx.bind()
+
+
+def _ptr(t: torch.Tensor | None):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+# ---------------------------------------------------------------------------
+# argument conversion, in the reference's terms
+# ---------------------------------------------------------------------------
+
+def to_device_f32(x, argno: int, name: str, device=None) -> torch.Tensor:
+    """A contiguous 1-D float32 CUDA tensor holding ``x``.
+
+    Like the reference's generated entry points, arrays must already be
+    float32; anything else raises TypeError (there is no silent cast).
+    Multi-dimensional inputs are flattened (the reference takes flattened
+    arrays, README.md:24).
+    """
+    if isinstance(x, torch.Tensor):
+        if x.dtype != torch.float32:
+            raise TypeError(f"Argument #{argno} ({name}) has invalid value\nFuthark type: []f32\n"
+                            f"Argument has torch dtype {x.dtype}")
+        dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        return x.reshape(-1).to(dev, non_blocking=True).contiguous()
+    if hasattr(x, "get") and not isinstance(x, np.ndarray):      # DeviceArray or a pyopencl-like array
+        if isinstance(x, DeviceArray):
+            return to_device_f32(x.torch(), argno, name, device)
+        x = x.get()
+    arr = np.asarray(x)
+    if arr.dtype != np.float32:
+        raise TypeError(f"Argument #{argno} ({name}) has invalid value\nFuthark type: []f32\n"
+                        f"Argument has Python type {type(x).__name__} and dtype {arr.dtype}")
+    t = torch.from_numpy(np.ascontiguousarray(arr.reshape(-1)))
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+    if t.numel() and not t.is_pinned():
+        return t.to(dev)
+    return t.to(dev, non_blocking=True)
+
+
+def scalar_f32(v, argno: int, name: str) -> float:
+    try:
+        f = np.float32(v)
+    except (TypeError, ValueError):
+        raise TypeError(f"Argument #{argno} ({name}) has invalid value\nFuthark type: f32\n"
+                        f"Argument has Python type {type(v).__name__} and value: {v!r}") from None
+    if isinstance(v, (np.ndarray,)) and np.ndim(v) != 0:
+        raise TypeError(f"Argument #{argno} ({name}) must be a scalar f32")
+    return float(f)
+
+
+def scalar_i32(v, argno: int, name: str) -> int:
+    if isinstance(v, (bool, np.bool_)) or not isinstance(v, (int, np.integer)):
+        if isinstance(v, (float, np.floating)) and float(v).is_integer():
+            v = int(v)
+        else:
+            raise TypeError(f"Argument #{argno} ({name}) has invalid value\nFuthark type: i32\n"
+                            f"Argument has Python type {type(v).__name__} and value: {v!r}")
+    iv = int(v)
+    if not (-2 ** 31 <= iv < 2 ** 31):
+        raise TypeError(f"Argument #{argno} ({name}) does not fit in i32: {iv}")
+    return iv
+
+
+class DeviceArray:
+    """Result of an entry point: a flattened float32 device array.
+
+    ``get()`` copies it to a NumPy array (as ``pyopencl.array.Array.get()``
+    does for the reference's generated classes) after checking that the
+    kernels that produced it completed without error.
+    """
+
+    def __init__(self, tensor: torch.Tensor, ctx: _Context):
+        self._t = tensor
+        self._ctx = ctx
+
+    def torch(self) -> torch.Tensor:
+        return self._t
+
+    def get(self) -> np.ndarray:
+        self._ctx.sync()
+        return self._t.detach().cpu().numpy()
+
+    @property
+    def shape(self):
+        return tuple(self._t.shape)
+
+    @property
+    def dtype(self):
+        return np.dtype(np.float32)
+
+    def __len__(self):
+        return self._t.numel()
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.get()
+        return a if dtype is None else a.astype(dtype)
+
+    def __repr__(self):
+        return f"DeviceArray(shape={self.shape}, dtype=float32, device={self._t.device})"
+
+
+# ---------------------------------------------------------------------------
+# operations on device tensors
+# ---------------------------------------------------------------------------
+
+def forwardprojection(angles: torch.Tensor, rhozero: float, deltarho: float, numrhos: int, image: torch.Tensor,
+                      out: torch.Tensor | None = None, sparse: bool = False) -> torch.Tensor:
+    """Angle-major sinogram [a*numrhos] of ``image`` (futhark/forwardprojection.fut:71-84)."""
+    ctx = context(image.device.index)
+    a = angles.numel()
+    if out is None:
+        out = torch.empty(a * int(numrhos), dtype=torch.float32, device=image.device)
+    fn = ctx.lib.synk_forwardprojection_sparse if sparse else ctx.lib.synk_forwardprojection
+    rc = fn(ctx.handle, _ptr(out), _ptr(angles), a, rhozero, deltarho, int(numrhos), _ptr(image), image.numel())
+    ctx.check(rc, "forwardprojection")
+    return out
+
+
+def backprojection(angles: torch.Tensor, rhozero: float, deltarho: float, size: int, projections: torch.Tensor,
+                   out: torch.Tensor | None = None, sparse: bool = False) -> torch.Tensor:
+    """Image [size*size] backprojected from ``projections`` (futhark/backprojection.fut:82-93)."""
+    ctx = context(projections.device.index)
+    a = angles.numel()
+    side = (int(size) // 2) * 2
+    if out is None:
+        out = torch.empty(side * side, dtype=torch.float32, device=projections.device)
+    fn = ctx.lib.synk_backprojection_sparse if sparse else ctx.lib.synk_backprojection
+    rc = fn(ctx.handle, _ptr(out), _ptr(angles), a, rhozero, deltarho, int(size), _ptr(projections),
+            projections.numel())
+    ctx.check(rc, "backprojection")
+    return out
+
+
+def sirt_slices(angles: torch.Tensor, rhozero: float, deltarho: float, numrhos: int, size: int, nslices: int,
+                image: torch.Tensor | None, projections: torch.Tensor, iterations: int, tol: float = 0.0,
+                residuals: bool = False, fp_split: int = 0, bp_split: int = 0,
+                out: torch.Tensor | None = None):
+    """SIRT of ``nslices`` independent slices in one persistent launch.
+
+    Returns ``(x, res, done)``: x [nslices*size*size]; res [nslices,
+    iterations+1] relative residuals ||FP(x_k)-b||/||b|| (float64, None unless
+    ``residuals``); done [nslices] number of updates applied (int32).
+    """
+    ctx = context(projections.device.index)
+    dev = projections.device
+    n = int(size) * int(size)
+    if out is None:
+        out = torch.empty(int(nslices) * n, dtype=torch.float32, device=dev)
+    res = None
+    if residuals:
+        res = torch.full((int(nslices), int(iterations) + 1), float("nan"), dtype=torch.float64, device=dev)
+    done = torch.zeros(int(nslices), dtype=torch.int32, device=dev)
+    opts = _lib.SynkOptions(float(tol), res.data_ptr() if res is not None else None, done.data_ptr(),
+                            int(fp_split), int(bp_split))
+    rc = ctx.lib.synk_sirt_slices(ctx.handle, _ptr(out), _ptr(angles), angles.numel(), rhozero, deltarho,
+                                  int(numrhos), int(size), int(nslices), _ptr(image), _ptr(projections),
+                                  int(iterations), ctypes.byref(opts))
+    ctx.check(rc, "sirt")
+    return out, res, done
+
+
+def sirt(angles: torch.Tensor, rhozero: float, deltarho: float, image: torch.Tensor, projections: torch.Tensor,
+         iterations: int, out: torch.Tensor | None = None) -> torch.Tensor:
+    """``iterations`` SIRT updates from ``image`` (futhark/SIRT.fut:43-49)."""
+    ctx = context(projections.device.index)
+    if out is None:
+        out = torch.empty(image.numel(), dtype=torch.float32, device=projections.device)
+    rc = ctx.lib.synk_SIRT(ctx.handle, _ptr(out), _ptr(angles), angles.numel(), rhozero, deltarho, _ptr(image),
+                           image.numel(), _ptr(projections), projections.numel(), int(iterations))
+    ctx.check(rc, "SIRT")
+    return out
+
+
+def sirt3d(angles: torch.Tensor, rhos: torch.Tensor, projections: torch.Tensor, iterations: int, size: int,
+           out: torch.Tensor | None = None) -> torch.Tensor:
+    """``size`` slices reconstructed independently (futhark/SIRT3D.fut:18-29)."""
+    ctx = context(projections.device.index)
+    if out is None:
+        out = torch.empty(int(size) ** 3, dtype=torch.float32, device=projections.device)
+    rc = ctx.lib.synk_SIRT3D(ctx.handle, _ptr(out), _ptr(angles), angles.numel(), _ptr(rhos), rhos.numel(),
+                             _ptr(projections), projections.numel(), int(iterations), int(size))
+    ctx.check(rc, "SIRT3D")
+    return out
+
+
+def image_side(n: int) -> int:
+    s = math.isqrt(int(n))
+    return s

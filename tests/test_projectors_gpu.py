@@ -1,0 +1,127 @@
+"""Parity of the CUDA forward projector and backprojector with the oracle.
+
+The FP32 restatement (oracle/cpu_ref.c) carries the reference's float32
+rounding; the FP64 restatement (oracle/fut_ref.py) is the accuracy judge.
+Tolerance: relative L2 error <= 1e-5 against both, except where the oracle
+pair itself disagrees (geometries with rays running along pixel edges, where
+f32 rounding picks the column: there the CUDA path must follow the f32
+reference).
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cpu_ref
+from oracle import fut_ref as F
+from synkrotomo_gb300 import phantom
+from synkrotomo_gb300 import runtime as rt
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+GEOMS = [
+    # (size, angles, numrhos, deltarho, arc)
+    (16, 12, None, 1.0, math.pi),       # integer rhozero, theta = pi/2 on pixel edges
+    (32, 30, None, 1.0, math.pi),
+    (64, 64, None, 1.0, math.pi),
+    (128, 128, None, 1.0, math.pi),     # the SIRT configuration's geometry
+    (64, 1, None, 1.0, math.pi),        # single angle
+    (64, 95, None, 1.0, math.pi),       # sparse-view upper end
+    (48, 40, 100, 1.0, math.pi),        # detectors wider than the image
+    (48, 40, 30, 1.0, math.pi),         # detectors narrower than the image
+    (40, 36, None, 0.5, math.pi),       # rhosprpixel = 3
+    (40, 36, 41, 1.5, math.pi),         # rhosprpixel = 1
+    (32, 33, None, 1.0, 2 * math.pi),   # full circle: negative cos and sin
+    (36, 60, None, 1.0, 2 * math.pi / 3),  # limited angle
+]
+
+
+def _dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def _geom(size, a, nr, dr, arc):
+    return phantom.geometry(size, a, numrhos=nr, deltarho=dr, arc=arc)
+
+
+@pytest.mark.parametrize("size,a,nr,dr,arc", GEOMS)
+def test_forwardprojection_matches_oracle(gpu, size, a, nr, dr, arc):
+    g = _geom(size, a, nr, dr, arc)
+    img = phantom.ellipse_phantom(size, seed=size + a)
+    out = rt.forwardprojection(_dev(g.angles), g.rhozero, g.deltarho, g.numrhos, _dev(img)).cpu().numpy()
+    ref32 = cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, img)
+    assert out.shape == (a * g.numrhos,)
+    assert rel_l2(out, ref32) < TOL
+    ref64 = F.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, img)
+    if rel_l2(ref32, ref64) < TOL:
+        assert rel_l2(out, ref64) < TOL
+    # elementwise: no ray off by more than a rounding-level amount
+    assert np.max(np.abs(out - ref32)) <= 1e-4 * max(1.0, float(np.max(np.abs(ref32))))
+
+
+@pytest.mark.parametrize("size,a,nr,dr,arc", GEOMS)
+def test_backprojection_matches_oracle(gpu, size, a, nr, dr, arc):
+    g = _geom(size, a, nr, dr, arc)
+    y = np.random.default_rng(size * a).random(g.n_rays).astype(np.float32)
+    out = rt.backprojection(_dev(g.angles), g.rhozero, g.deltarho, size, _dev(y)).cpu().numpy()
+    ref32 = cpu_ref.backprojection(g.angles, g.rhozero, g.deltarho, size, y)
+    assert out.shape == (size * size,)
+    assert rel_l2(out, ref32) < TOL
+    ref64 = F.backprojection(g.angles, g.rhozero, g.deltarho, size, y)
+    if rel_l2(ref32, ref64) < TOL:
+        assert rel_l2(out, ref64) < TOL
+    assert np.max(np.abs(out - ref32)) <= 1e-4 * max(1.0, float(np.max(np.abs(ref32))))
+
+
+def test_edge_rays_follow_the_f32_reference(gpu):
+    # theta = f32(pi/2) with integer rhozero: the f32 reference assigns the
+    # whole ray to one column, FP64 to its neighbour; the CUDA path follows f32.
+    size = 16
+    ang = np.array([np.float32(math.pi / 2)], np.float32)
+    img = np.arange(size * size, dtype=np.float32) / 100.0
+    out = rt.forwardprojection(_dev(ang), -11.0, 1.0, 23, _dev(img)).cpu().numpy()
+    ref32 = cpu_ref.forwardprojection(ang, -11.0, 1.0, 23, img)
+    np.testing.assert_allclose(out, ref32, rtol=1e-6, atol=1e-5)
+    ref64 = F.forwardprojection(ang, -11.0, 1.0, 23, img)
+    assert rel_l2(ref32, ref64) > 1e-3   # the oracle pair disagrees here by design
+
+
+def test_projectors_are_linear_and_adjoint(gpu):
+    # size-independent properties at a large size (the oracle would take minutes)
+    size, a = 512, 180
+    g = phantom.geometry(size, a, numrhos=726)   # half-integer rhozero: exact adjoint pair
+    rng = np.random.default_rng(5)
+    x1 = _dev(rng.random(size * size).astype(np.float32))
+    x2 = _dev(rng.random(size * size).astype(np.float32))
+    y = _dev(rng.random(g.n_rays).astype(np.float32))
+    ang = _dev(g.angles)
+    f1 = rt.forwardprojection(ang, g.rhozero, g.deltarho, g.numrhos, x1)
+    f2 = rt.forwardprojection(ang, g.rhozero, g.deltarho, g.numrhos, x2)
+    f12 = rt.forwardprojection(ang, g.rhozero, g.deltarho, g.numrhos, 2.0 * x1 + x2)
+    assert rel_l2(f12.cpu().numpy(), (2.0 * f1 + f2).cpu().numpy()) < 1e-5
+    bt = rt.backprojection(ang, g.rhozero, g.deltarho, size, y)
+    lhs = float(torch.dot(f1.double(), y.double()))
+    rhs = float(torch.dot(x1.double(), bt.double()))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # A*1 of the central ray of angle 0 is the image height
+    ones = torch.ones(size * size, device="cuda")
+    a1 = rt.forwardprojection(_dev(np.zeros(1, np.float32)), -0.5, 1.0, 2, ones).cpu().numpy()
+    np.testing.assert_allclose(a1, [size, size], rtol=1e-6)
+
+
+def test_large_geometry_against_fp64_oracle_sample(gpu):
+    # N=512 with the detector count of the reference's rad512 dataset (725,
+    # integer rhozero); a sample of angles keeps the oracle quick
+    size = 512
+    angles = np.linspace(0.0, math.pi, 2048, endpoint=False).astype(np.float32)[::97].copy()
+    rhozero, nr = -362.0, 725
+    img = phantom.ellipse_phantom(size, seed=11)
+    out = rt.forwardprojection(_dev(angles), rhozero, 1.0, nr, _dev(img)).cpu().numpy()
+    ref32 = cpu_ref.forwardprojection(angles, rhozero, 1.0, nr, img)
+    ref64 = F.forwardprojection(angles, rhozero, 1.0, nr, img)
+    assert rel_l2(out, ref32) < TOL
+    assert rel_l2(out, ref64) < TOL

@@ -1,0 +1,113 @@
+"""Parity of the persistent CUDA SIRT with the oracle.
+
+Bar (from the project's accuracy targets): plain SIRT within 1e-5 relative L2
+of the FP32 reference and within 1e-4 of the FP64 oracle.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cpu_ref
+from oracle import fut_ref as F
+from synkrotomo_gb300 import phantom
+from synkrotomo_gb300 import runtime as rt
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def _problem(size, a, seed, nr=None, noise=0.01, arc=math.pi):
+    g = phantom.geometry(size, a, numrhos=nr, arc=arc)
+    img = phantom.ellipse_phantom(size, seed)
+    b = cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, img)
+    if noise:
+        b = phantom.add_noise(b, seed, noise)
+    return g, img, b
+
+
+def test_sirt_config0_parity(gpu):
+    """N=128, 128 angles, 182 detectors, 1 % noise, 200 iterations."""
+    g, _, b = _problem(128, 128, seed=0)
+    x0 = np.zeros(128 * 128, np.float32)
+    x = rt.sirt(_dev(g.angles), g.rhozero, g.deltarho, _dev(x0), _dev(b), 200).cpu().numpy()
+    ref32 = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, x0, b, 200)
+    ops = F.SirtOperators(g.angles, g.rhozero, g.deltarho, g.numrhos, 128)
+    ref64 = ops.iterate(x0, b, 200)
+    assert rel_l2(x, ref32) < 1e-5
+    assert rel_l2(x, ref64) < 1e-4
+
+
+@pytest.mark.parametrize("size,a,nr,its", [(16, 12, None, 20), (32, 30, None, 50), (64, 17, 91, 30), (24, 40, 60, 25)])
+def test_sirt_small_geometries(gpu, size, a, nr, its):
+    g, img, b = _problem(size, a, seed=size, nr=nr)
+    x0 = (0.1 * img).astype(np.float32)       # a non-zero start
+    x = rt.sirt(_dev(g.angles), g.rhozero, g.deltarho, _dev(x0), _dev(b), its).cpu().numpy()
+    ref32 = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, x0, b, its)
+    assert rel_l2(x, ref32) < 1e-5
+
+
+def test_sirt_zero_iterations_returns_start(gpu):
+    g, img, b = _problem(32, 10, seed=2)
+    x = rt.sirt(_dev(g.angles), g.rhozero, g.deltarho, _dev(img), _dev(b), 0).cpu().numpy()
+    np.testing.assert_array_equal(x, img)
+
+
+@pytest.mark.parametrize("fs,bs", [(1, 1), (2, 4), (8, 8), (4, 2)])
+def test_work_splits_agree(gpu, fs, bs):
+    g, _, b = _problem(64, 48, seed=4)
+    ang, bd = _dev(g.angles), _dev(b)
+    x, res, done = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, 64, 1, None, bd, 40,
+                                  fp_split=fs, bp_split=bs, residuals=True)
+    ref32 = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(64 * 64, np.float32), b, 40)
+    assert rel_l2(x.cpu().numpy(), ref32) < 1e-5
+    assert int(done.item()) == 40
+
+
+def test_residual_history_and_stopping_rule(gpu):
+    g, _, b = _problem(64, 60, seed=7, noise=0.0)
+    ang, bd = _dev(g.angles), _dev(b)
+    x, res, done = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, 64, 1, None, bd, 60, residuals=True)
+    ops = F.SirtOperators(g.angles, g.rhozero, g.deltarho, g.numrhos, 64)
+    hist = []
+    ops.iterate(np.zeros(64 * 64, np.float32), b, 60, hist)
+    r = res.cpu().numpy()[0]
+    np.testing.assert_allclose(r, hist, rtol=1e-4)
+    # stop at the first iterate whose residual is below the 20th iterate's
+    tol = float(hist[20]) * 1.0001
+    x2, res2, done2 = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, 64, 1, None, bd, 60, tol=tol,
+                                     residuals=True)
+    k = int(done2.item())
+    assert k == next(i for i, v in enumerate(hist) if v <= tol)
+    xk = ops.iterate(np.zeros(64 * 64, np.float32), b, k)
+    assert rel_l2(x2.cpu().numpy(), xk) < 1e-4
+
+
+def test_sirt_slices_match_single_slice_runs(gpu):
+    size, a, ns = 32, 24, 5
+    g = phantom.geometry(size, a)
+    vol = phantom.ellipsoid_volume(size, ns, seed=1)
+    sinos = np.stack([cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, vol[i])
+                      for i in range(ns)])
+    x, _, _ = rt.sirt_slices(_dev(g.angles), g.rhozero, g.deltarho, g.numrhos, size, ns, None,
+                             _dev(sinos.ravel()), 15)
+    x = x.cpu().numpy().reshape(ns, -1)
+    for i in range(ns):
+        ref = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), sinos[i], 15)
+        assert rel_l2(x[i], ref) < 1e-5
+
+
+def test_sirt3d_matches_reference_semantics(gpu):
+    size, a = 16, 10
+    g = phantom.geometry(size, a, numrhos=24)
+    rhos = (g.rhozero + np.arange(24) * g.deltarho).astype(np.float32)
+    proj = np.random.default_rng(3).random(size * a * 24).astype(np.float32)
+    x = rt.sirt3d(_dev(g.angles), _dev(rhos), _dev(proj), 8, size).cpu().numpy()
+    ref = cpu_ref.sirt3d(g.angles, rhos, proj, 8, size)
+    assert x.shape == (size ** 3,)
+    assert rel_l2(x, ref) < 1e-5
