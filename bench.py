@@ -402,7 +402,7 @@ def main():
                        "step": "forward projection + backprojection", "l2": "flushed (512 MB write) before every step",
                        "parallelism": f"replicas x{world}"},
             "fp_ms": res["fp_ms"], "bp_ms": res["bp_ms"],
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": 8 * args.steps,
             "clocks": res["clocks"], "roofline": roofline}
     e = res["e2e"]
     line["e2e"] = {"value": world * step_bytes() / (e["ms"] * 1e-3) / 1e9, "unit": "GB/s",

@@ -125,6 +125,29 @@ int synk_sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t
                      float deltarho, int32_t numrhos, int32_t size, int32_t nslices, const float *image,
                      const float *projections, int32_t iterations, const synk_sirt_options *opts);
 
+/* ---- CSR system matrix (no reference counterpart) ----
+ * The forward projector's rule (futhark/forwardprojection.fut:31-56) stored
+ * as a sparse matrix A (rows: rays k*numrhos + r, angle-major; columns:
+ * row-major pixels) together with its exact transpose A^T, both built on the
+ * GPU.  Row pointers are int64, column indices int32, values float32. */
+typedef struct synk_csr synk_csr;
+
+int synk_csr_new(synk_context *ctx, synk_csr **out, const float *angles, int64_t a, float rhozero, float deltarho,
+                 int32_t numrhos, int32_t size);
+void synk_csr_free(synk_csr *m);
+/* rows = a*numrhos, cols = size*size, nnz = non-zeros of A (= of A^T). */
+int synk_csr_shape(const synk_csr *m, int64_t *rows, int64_t *cols, int64_t *nnz);
+/* Device arrays of A (transpose = 0) or A^T (transpose = 1). */
+int synk_csr_arrays(const synk_csr *m, int transpose, const int64_t **rowptr, const int32_t **colidx,
+                    const float **vals);
+/* y[rows] = A x[cols] */
+int synk_csr_spmv(synk_context *ctx, const synk_csr *m, const float *x, float *y);
+/* x[cols] = A^T y[rows] */
+int synk_csr_spmv_t(synk_context *ctx, const synk_csr *m, const float *y, float *x);
+/* y[rows] = M x for a caller-owned CSR matrix (int32 row pointers). */
+int synk_spmv_csr32(synk_context *ctx, int64_t rows, const int32_t *rowptr, const int32_t *colidx,
+                    const float *vals, const float *x, float *y);
+
 #ifdef __cplusplus
 }
 #endif

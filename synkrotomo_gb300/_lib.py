@@ -63,6 +63,17 @@ SIGNATURES = {
                                         ctypes.c_float, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                         ctypes.POINTER(SynkOptions)]),
+    "synk_csr_new": (ctypes.c_int, [c_ctx, ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_int32]),
+    "synk_csr_free": (None, [ctypes.c_void_p]),
+    "synk_csr_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "synk_csr_arrays": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
+    "synk_csr_spmv": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "synk_csr_spmv_t": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "synk_spmv_csr32": (ctypes.c_int, [c_ctx, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 

@@ -10,8 +10,18 @@
 
 #include "synk_internal.cuh"
 #include "sirt_internal.cuh"
+#include "csr_internal.cuh"
+#include "fp_tile.cuh"
 
 using namespace synk;
+
+struct synk_csr {
+    int device = 0;
+    int64_t rows = 0, cols = 0, nnz = 0;
+    int64_t *ptr = nullptr, *ptr_t = nullptr;
+    int *idx = nullptr, *idx_t = nullptr;
+    float *vals = nullptr, *vals_t = nullptr;
+};
 
 struct synk_context {
     int device = 0;
@@ -134,6 +144,20 @@ int pick_split(long long tasks, long long resident_warps, int max_split) {
     return s;
 }
 
+// Angle lists of a geometry in scratch memory: order[a + 64], exact[a], counts[3].
+cudaError_t make_lists(Scratch &sc, const ProbGeom &P, AngleLists *L, cudaStream_t st) {
+    int *order, *exact, *counts;
+    cudaError_t e;
+    if ((e = sc.get(&order, (size_t)P.a + 64)) != cudaSuccess) return e;
+    if ((e = sc.get(&exact, (size_t)P.a)) != cudaSuccess) return e;
+    if ((e = sc.get(&counts, 4)) != cudaSuccess) return e;
+    if ((e = launch_angle_lists(P, order, exact, counts, st)) != cudaSuccess) return e;
+    L->order = order;
+    L->exact = exact;
+    L->counts = counts;
+    return cudaSuccess;
+}
+
 int forward(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero, float deltarho,
             int32_t numrhos, const float *image, int64_t n) {
     int rc = check_ctx(ctx);
@@ -142,15 +166,19 @@ int forward(synk_context *ctx, float *out, const float *angles, int64_t a, float
     int64_t size = 0;
     if ((rc = image_side(ctx, n, &size))) return rc;
     if ((rc = check_geometry(ctx, a, rhozero, deltarho, numrhos, size))) return rc;
-    Scratch sc(ctx->stream);
+    cudaStream_t st = ctx->stream;
+    Scratch sc(st);
     AngleGeom *geom;
-    float *imgT;
+    float *xpad, *xTpad;
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
-    SYNK_CUDA(sc.get(&imgT, (size_t)n), "cudaMallocAsync(transposed image)");
-    SYNK_CUDA(launch_geometry(angles, (int)a, geom, ctx->stream), "geometry kernel");
-    SYNK_CUDA(launch_transpose(image, imgT, (int)size, 1, ctx->stream), "transpose kernel");
+    SYNK_CUDA(sc.get(&xpad, (size_t)size * (size + 2)), "cudaMallocAsync(padded image)");
+    SYNK_CUDA(sc.get(&xTpad, (size_t)size * (size + 2)), "cudaMallocAsync(padded transposed image)");
+    SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size, geom);
-    SYNK_CUDA(launch_fp(P, image, imgT, out, ctx->stream), "forward projection kernel");
+    AngleLists L;
+    SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
+    SYNK_CUDA(launch_pad(image, xpad, xTpad, (int)size, 1, st), "pad kernel");
+    SYNK_CUDA(launch_fp(P, L, xpad, xTpad, out, st), "forward projection kernel");
     return SYNK_OK;
 }
 
@@ -164,12 +192,15 @@ int backward(synk_context *ctx, float *out, const float *angles, int64_t a, floa
                                     (long long)p, (long long)a);
     const int64_t numrhos = p / a;
     if ((rc = check_geometry(ctx, a, rhozero, deltarho, numrhos, size_in))) return rc;
-    Scratch sc(ctx->stream);
+    cudaStream_t st = ctx->stream;
+    Scratch sc(st);
     AngleGeom *geom;
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
-    SYNK_CUDA(launch_geometry(angles, (int)a, geom, ctx->stream), "geometry kernel");
+    SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size_in, geom);
-    SYNK_CUDA(launch_bp(P, projections, out, ctx->stream), "backprojection kernel");
+    AngleLists L;
+    SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
+    SYNK_CUDA(launch_bp(P, L, projections, out, st), "backprojection kernel");
     return SYNK_OK;
 }
 
@@ -199,15 +230,17 @@ int sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, f
     }
     Scratch sc(st);
     AngleGeom *geom;
-    float *R, *C, *xT, *rr;
+    float *R, *C, *xpad, *xTpad, *rr;
     double *res2, *b2;
     int *stop_iter;
     unsigned *words;
     const size_t K = (size_t)iterations + 1;
+    const size_t np = (size_t)size * (size + 2);
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync");
     SYNK_CUDA(sc.get(&R, pr), "cudaMallocAsync(R)");
     SYNK_CUDA(sc.get(&C, n), "cudaMallocAsync(C)");
-    SYNK_CUDA(sc.get(&xT, n * nslices), "cudaMallocAsync(xT)");
+    SYNK_CUDA(sc.get(&xpad, np * nslices), "cudaMallocAsync(padded image)");
+    SYNK_CUDA(sc.get(&xTpad, np * nslices), "cudaMallocAsync(padded transposed image)");
     SYNK_CUDA(sc.get(&rr, pr * nslices), "cudaMallocAsync(residual)");
     SYNK_CUDA(sc.get(&res2, K * nslices), "cudaMallocAsync");
     SYNK_CUDA(sc.get(&b2, (size_t)nslices), "cudaMallocAsync");
@@ -220,23 +253,25 @@ int sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, f
     SYNK_CUDA(cudaGetLastError(), "fill kernel");
     SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size, geom);
+    AngleLists L;
+    SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
     SYNK_CUDA(launch_normalisers(P, R, C, st), "normaliser kernels");
-    SYNK_CUDA(launch_transpose(out, xT, (int)size, (int)nslices, st), "transpose kernel");
+    SYNK_CUDA(launch_pad(out, xpad, xTpad, (int)size, (int)nslices, st), "pad kernel");
     SYNK_CUDA(launch_sumsq(projections, pr, (int)nslices, b2, st), "norm kernel");
 
     SirtParams sp;
     sp.P = P;
     sp.R = R;
     sp.C = C;
+    sp.L = L;
     sp.b = projections;
-    sp.x = out;
-    sp.xT = xT;
+    sp.xpad = xpad;
+    sp.xTpad = xTpad;
     sp.rr = rr;
     sp.res2 = res2;
     sp.b2 = b2;
     sp.stop_iter = stop_iter;
     sp.bar = words;
-    sp.work = words + 4;
     sp.status = ctx->d_status;
     sp.timeout_ns = ctx->barrier_timeout_ns;
     sp.tol2 = (opts && opts->tol > 0.0) ? opts->tol * opts->tol : 0.0;
@@ -247,8 +282,9 @@ int sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, f
     const int grid = sirt_persistent_grid(&bps);
     if (grid < 1) return fail(ctx, SYNK_ECUDA, "persistent SIRT kernel cannot be resident");
     const long long resident_warps = (long long)grid * 8;
-    const long long fp_tasks = (long long)nslices * a * ((numrhos + 31) / 32);
-    const long long bp_tasks = (long long)nslices * size * ((size + 31) / 32);
+    // warp tasks per phase: one detector x 32 angles (FP), one 32-column x 4-row strip (BP)
+    const long long fp_tasks = (long long)nslices * numrhos * ((a + 31) / 32);
+    const long long bp_tasks = (long long)nslices * ((size + 3) / 4) * ((size + 31) / 32);
     int fs = opts && opts->fp_split > 0 ? opts->fp_split : pick_split(fp_tasks, resident_warps, (int)(size / 16 > 8 ? 8 : (size / 16 < 1 ? 1 : size / 16)));
     int bs = opts && opts->bp_split > 0 ? opts->bp_split : pick_split(bp_tasks, resident_warps, (int)(a / 8 > 8 ? 8 : (a / 8 < 1 ? 1 : a / 8)));
     if (fs != 1 && fs != 2 && fs != 4 && fs != 8) return fail(ctx, SYNK_EINVAL, "fp_split must be 1, 2, 4 or 8");
@@ -256,6 +292,7 @@ int sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, f
     sp.fp_split = fs;
     sp.bp_split = bs;
     SYNK_CUDA(launch_sirt_persistent(sp, grid, st), "persistent SIRT kernel");
+    SYNK_CUDA(launch_unpad(xpad, out, (int)size, (int)nslices, st), "unpad kernel");
     if (opts && (opts->residuals || opts->iterations_done))
         SYNK_CUDA(launch_sirt_finalize(sp, opts->residuals, opts->iterations_done, st), "finalize kernel");
     return SYNK_OK;
@@ -274,6 +311,14 @@ int synk_context_new(synk_context **out, int device, void *stream) {
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return SYNK_ECUDA;
     if (device < 0 || device >= ndev) return SYNK_EINVAL;
     if (cudaSetDevice(device) != cudaSuccess) return SYNK_ECUDA;
+    // Keep freed stream-ordered scratch in the device's default pool instead of
+    // returning it to the driver at every synchronisation (the default release
+    // threshold 0 makes each call re-map its scratch).
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     synk_context *ctx = new synk_context();
     ctx->device = device;
     ctx->stream = static_cast<cudaStream_t>(stream);
@@ -375,6 +420,125 @@ int synk_sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t
     if (rc) return rc;
     return sirt_slices(ctx, out, angles, a, rhozero, deltarho, numrhos, size, nslices, image, projections,
                        iterations, opts);
+}
+
+static void csr_release(synk_csr *m) {
+    if (!m) return;
+    cudaFree(m->ptr); cudaFree(m->ptr_t);
+    cudaFree(m->idx); cudaFree(m->idx_t);
+    cudaFree(m->vals); cudaFree(m->vals_t);
+    delete m;
+}
+
+int synk_csr_new(synk_context *ctx, synk_csr **out, const float *angles, int64_t a, float rhozero, float deltarho,
+                 int32_t numrhos, int32_t size) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out || !angles) return fail(ctx, SYNK_EINVAL, "null pointer");
+    *out = nullptr;
+    if ((rc = check_geometry(ctx, a, rhozero, deltarho, numrhos, size))) return rc;
+    const int64_t rows = a * (int64_t)numrhos, cols = (int64_t)size * size;
+    if (rows >= (1ll << 31) || cols >= (1ll << 31))
+        return fail(ctx, SYNK_EINVAL, "matrix dimensions exceed int32 indices");
+    cudaStream_t st = ctx->stream;
+    synk_csr *m = new synk_csr();
+    m->device = ctx->device;
+    m->rows = rows;
+    m->cols = cols;
+    Scratch sc(st);
+    AngleGeom *geom;
+    int *counts;
+    int64_t *sums, *total;
+    const int64_t maxn = rows > cols ? rows : cols;
+    cudaError_t e;
+#define CSR_TRY(call, what)                         \
+    do {                                            \
+        e = (call);                                 \
+        if (e != cudaSuccess) {                     \
+            csr_release(m);                         \
+            return cuda_fail(ctx, e, what);         \
+        }                                           \
+    } while (0)
+    CSR_TRY(sc.get(&geom, (size_t)a), "cudaMallocAsync");
+    CSR_TRY(sc.get(&counts, (size_t)maxn), "cudaMallocAsync");
+    CSR_TRY(sc.get(&sums, (size_t)(maxn / 1024 + 2)), "cudaMallocAsync");
+    CSR_TRY(sc.get(&total, 2), "cudaMallocAsync");
+    CSR_TRY(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
+    const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size, geom);
+    for (int tr = 0; tr < 2; ++tr) {
+        const int64_t n = tr ? cols : rows;
+        int64_t **pp = tr ? &m->ptr_t : &m->ptr;
+        int **ip = tr ? &m->idx_t : &m->idx;
+        float **vp = tr ? &m->vals_t : &m->vals;
+        CSR_TRY(cudaMalloc(pp, sizeof(int64_t) * (n + 1)), "cudaMalloc(row pointers)");
+        CSR_TRY(launch_csr_count(P, tr != 0, counts, st), "count kernel");
+        CSR_TRY(exclusive_scan(counts, n, *pp, sums, total, st), "scan kernels");
+        int64_t nnz = 0;
+        CSR_TRY(cudaMemcpyAsync(&nnz, total, sizeof nnz, cudaMemcpyDeviceToHost, st), "read nnz");
+        CSR_TRY(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        if (tr && nnz != m->nnz) {
+            csr_release(m);
+            return fail(ctx, SYNK_ECUDA, "transpose has %lld non-zeros, A has %lld", (long long)nnz, (long long)m->nnz);
+        }
+        m->nnz = nnz;
+        CSR_TRY(cudaMalloc(ip, sizeof(int) * (nnz + 1)), "cudaMalloc(indices)");
+        CSR_TRY(cudaMalloc(vp, sizeof(float) * (nnz + 1)), "cudaMalloc(values)");
+        CSR_TRY(launch_csr_fill(P, tr != 0, *pp, *ip, *vp, st), "fill kernel");
+    }
+#undef CSR_TRY
+    *out = m;
+    return SYNK_OK;
+}
+
+void synk_csr_free(synk_csr *m) {
+    if (!m) return;
+    cudaSetDevice(m->device);
+    cudaDeviceSynchronize();
+    csr_release(m);
+}
+
+int synk_csr_shape(const synk_csr *m, int64_t *rows, int64_t *cols, int64_t *nnz) {
+    if (!m) return SYNK_EINVAL;
+    if (rows) *rows = m->rows;
+    if (cols) *cols = m->cols;
+    if (nnz) *nnz = m->nnz;
+    return SYNK_OK;
+}
+
+int synk_csr_arrays(const synk_csr *m, int transpose, const int64_t **rowptr, const int32_t **colidx,
+                    const float **vals) {
+    if (!m) return SYNK_EINVAL;
+    if (rowptr) *rowptr = transpose ? m->ptr_t : m->ptr;
+    if (colidx) *colidx = transpose ? m->idx_t : m->idx;
+    if (vals) *vals = transpose ? m->vals_t : m->vals;
+    return SYNK_OK;
+}
+
+int synk_csr_spmv(synk_context *ctx, const synk_csr *m, const float *x, float *y) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!m || !x || !y) return fail(ctx, SYNK_EINVAL, "null pointer");
+    SYNK_CUDA(launch_spmv(m->rows, m->ptr, nullptr, m->idx, m->vals, x, y, ctx->stream), "spmv kernel");
+    return SYNK_OK;
+}
+
+int synk_csr_spmv_t(synk_context *ctx, const synk_csr *m, const float *y, float *x) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!m || !x || !y) return fail(ctx, SYNK_EINVAL, "null pointer");
+    SYNK_CUDA(launch_spmv(m->cols, m->ptr_t, nullptr, m->idx_t, m->vals_t, y, x, ctx->stream), "spmv kernel");
+    return SYNK_OK;
+}
+
+int synk_spmv_csr32(synk_context *ctx, int64_t rows, const int32_t *rowptr, const int32_t *colidx,
+                    const float *vals, const float *x, float *y) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (rows < 0) return fail(ctx, SYNK_EINVAL, "negative row count");
+    if (rows == 0) return SYNK_OK;
+    if (!rowptr || !colidx || !vals || !x || !y) return fail(ctx, SYNK_EINVAL, "null pointer");
+    SYNK_CUDA(launch_spmv(rows, nullptr, rowptr, colidx, vals, x, y, ctx->stream), "spmv kernel");
+    return SYNK_OK;
 }
 
 }  // extern "C"

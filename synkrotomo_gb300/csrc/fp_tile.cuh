@@ -1,0 +1,106 @@
+// Ray-driven forward projection with one lane per angle, shared by the
+// standalone forward projector and the persistent SIRT kernel.
+//
+// A warp owns one detector index r and 32 angles of the same class (all steep
+// or all flat, none near-axis).  The 32 rays of neighbouring angles at the
+// same detector cross almost the same pixels of a frame row, so each of the
+// warp's two gathers per row touches 2-3 sectors (lanes on adjacent detectors
+// of one angle would span ~45 columns).  Images are read from a padded copy
+// (row stride N+2, a zero column on each side) so one predicate covers both
+// pixels of a row segment.  Per lane and row (forwardprojection.fut:31-56):
+//   u  = j*slope + u0                  left end of the row segment, pixel units
+//   c  = floor(u), t = max(0, (u - c + |slope| - 1) / |slope|)   share of c+1
+//   s += v[c] + t*(v[c+1] - v[c])      (times lbase once per ray)
+// Near-axis angles are listed separately and run the reference's own
+// expressions (fp_exact in project.cu / the SIRT kernel).
+#pragma once
+
+#include "synk_internal.cuh"
+
+namespace synk {
+
+// Angle order of the lane-per-angle projector (built by angle_lists_kernel):
+//   order[g*32 + lane]: angle of lane in group g, -1 for an idle lane;
+//   groups [0, counts[0]) are steep, [counts[0], counts[0]+counts[1]) flat;
+//   exact[0 .. counts[2]): the near-axis angles.
+struct AngleLists {
+    const int *order;
+    const int *exact;
+    const int *counts;   // device: steep groups, flat groups, near-axis angles
+};
+
+// Row range [j0, j1) in which the ray's segment can touch a column of [0, N).
+__device__ __forceinline__ void lane_rows(const ProbGeom &P, const AngleGeom &g, float u0, int &j0, int &j1) {
+    j0 = 0;
+    j1 = P.N;
+    const float aslope = fabsf(g.slope);
+    if (g.slope != 0.0f) {
+        const float ja = (-1.0f - aslope - u0) / g.slope;
+        const float jb = ((float)P.N - u0) / g.slope;
+        const float lo = fmaxf(fminf(ja, jb) - 1.0f, 0.0f);
+        const float hi = fminf(fmaxf(ja, jb) + 2.0f, (float)P.N);
+        j0 = (int)lo;
+        j1 = (hi > lo) ? (int)hi : j0;
+    } else if (!(u0 > -1.0f && u0 < (float)P.N)) {
+        j1 = j0;
+    }
+}
+
+// Sum over frame rows [jb, je) of detector r for the lane's angle k (k < 0:
+// idle lane, returns 0).  img_pad: padded frame image (stride N+2, pixel
+// (j, c) at j*(N+2) + c + 1).  All 32 lanes of the warp must call it.
+__device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, const float *__restrict__ img_pad,
+                                             int jb, int je) {
+    const AngleGeom g = load_geom(P.geom, k >= 0 ? k : 0);
+    const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));    // forwardprojection.fut:28
+    const float intercept = __fdiv_rn(rho, g.cost);                               // forwardprojection.fut:29
+    const float u0 = ray_u0(P, g, intercept);
+    int j0 = 0, j1 = 0;
+    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, u0, j0, j1);
+    j0 = max(j0, jb);
+    j1 = min(j1, je);
+    if (j1 <= j0) { j0 = je; j1 = je; }
+    const int J0 = __reduce_min_sync(0xffffffffu, j0);
+    const int J1 = __reduce_max_sync(0xffffffffu, j1);
+    const float slope = g.slope, ainv = g.ainv;
+    const int stride = P.N + 2;
+    const unsigned lim = (unsigned)P.N;     // c + 1 in [0, N]
+    float sum = 0.0f, comp = 0.0f;
+    for (int j = J0; j < J1;) {
+        const int jend = min(j + 32, J1);
+        float part = 0.0f;
+#pragma unroll 4
+        for (; j < jend; ++j) {
+            const float u = fmaf((float)j, slope, u0);
+            int c;
+            const float fl = floor_magic(u, c);
+            const float t = right_share(u, fl, ainv);
+            const bool ok = (unsigned)(c + 1) <= lim;
+            const float *p = img_pad + (j * stride + c + 1);
+            const float v0 = ok ? __ldg(p) : 0.0f;
+            const float v1 = ok ? __ldg(p + 1) : 0.0f;
+            part += fmaf(t, v1 - v0, v0);
+        }
+        comp_add(sum, comp, part);
+    }
+    return k >= 0 ? (sum + comp) * g.lbase : 0.0f;
+}
+
+// Ray of a near-axis angle k over the whole frame, the reference's own
+// expressions (forwardprojection.fut:31-56), reading the padded frame.
+__device__ __forceinline__ float fp_exact_ray(const ProbGeom &P, int k, int r, const float *__restrict__ xpad,
+                                              const float *__restrict__ xTpad) {
+    const AngleGeom g = load_geom(P.geom, k);
+    const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));
+    if (fabsf(rho) > 0.75f * (float)P.N + 2.0f) return 0.0f;
+    const float intercept = __fdiv_rn(rho, g.cost);
+    float s;
+    fp_rows_exact<false>((g.flat ? xTpad : xpad) + 1, P.N + 2, P.half, g.slope, intercept, g.lbase, s);
+    return s;
+}
+
+cudaError_t launch_angle_lists(const ProbGeom &P, int *order, int *exact, int *counts, cudaStream_t stream);
+cudaError_t launch_pad(const float *x, float *xpad, float *xTpad, int N, int nslices, cudaStream_t stream);
+cudaError_t launch_unpad(const float *xpad, float *x, int N, int nslices, cudaStream_t stream);
+
+}  // namespace synk

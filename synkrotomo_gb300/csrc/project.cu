@@ -1,22 +1,18 @@
-// Projector kernels of libsynk: per-angle geometry table, image transpose,
-// ray-driven forward projector, pixel-driven backprojector and the SIRT
-// normalisers R = 1/(A*1), C = 1/(A^T*1).
+// Projector kernels of libsynk: per-angle geometry table, angle lists,
+// padded/transposed image copies, the forward projector
+// (futhark/forwardprojection.fut:21-84), the backprojector
+// (futhark/backprojection.fut:19-93) and the SIRT normalisers
+// R = 1/(A*1), C = 1/(A^T*1) (futhark/SIRT.fut:22-25).
 //
-// Forward projector (futhark/forwardprojection.fut:21-84): one thread per ray,
-// one warp per 32 consecutive detectors of one angle, eight angles per block
-// so that the eight warps of a block gather from overlapping image rows.  Flat
-// lines walk the transposed image, as the reference does, which keeps every
-// warp's gathers on one image row.
-//
-// Backprojector (futhark/backprojection.fut:19-93): one thread per pixel, a
-// 32 x 8 pixel tile per block, all angles in a loop; the pixel's chord with
-// each candidate ray is evaluated from the ray's distance to the pixel centre
-// (a trapezoid in rho), which is the reference's intersect_fact*lbase
-// (backprojection.fut:22-33, 62) without its per-detector divisions.
-// Near-axis lines keep the reference's own expressions (see geometry_kernel).
+//   forward:  fp_lane_kernel   one warp = one detector x 32 angles of one class
+//             fp_exact_kernel  near-axis angles, the reference's expressions
+//   backward: bp_tile_kernel   one block = 32 x 32 pixels, 4 per thread, all angles
+// See fp_tile.cuh and bp_tile.cuh for the per-ray and per-pixel arithmetic.
 #include <math.h>
 
 #include "synk_internal.cuh"
+#include "fp_tile.cuh"
+#include "bp_tile.cuh"
 
 namespace synk {
 
@@ -63,86 +59,216 @@ cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStr
     return cudaGetLastError();
 }
 
-// out[z][c][r] = in[z][r][c], N x N slices.
-__global__ void transpose_kernel(const float *__restrict__ in, float *__restrict__ out, int N) {
+// Ordered compaction of the angles into: steep fast-path angles (padded with
+// -1 to whole groups of 32), flat fast-path angles (padded likewise), and the
+// near-axis angles.  One block; deterministic order (ascending angle index).
+__global__ void __launch_bounds__(1024) angle_lists_kernel(const AngleGeom *__restrict__ geom, int a,
+                                                           int *__restrict__ order, int *__restrict__ exact,
+                                                           int *__restrict__ counts) {
+    __shared__ int sh[1024];
+    __shared__ int s_total;
+    int base_order = 0;
+    int nexact = 0;
+    for (int cls = 0; cls < 3; ++cls) {      // 0 steep, 1 flat, 2 near-axis
+        int base = 0;
+        for (int k0 = 0; k0 < a; k0 += 1024) {
+            const int k = k0 + threadIdx.x;
+            int f = 0;
+            if (k < a) {
+                const int fl = __ldg(reinterpret_cast<const int *>(geom + k) + 10);
+                const int ex = __ldg(reinterpret_cast<const int *>(geom + k) + 11);
+                f = cls == 2 ? ex : (!ex && fl == cls);
+            }
+            sh[threadIdx.x] = f;
+            __syncthreads();
+            for (int off = 1; off < 1024; off <<= 1) {
+                const int v = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+                __syncthreads();
+                sh[threadIdx.x] += v;
+                __syncthreads();
+            }
+            if (f) {
+                const int pos = base + sh[threadIdx.x] - 1;
+                if (cls == 2) exact[pos] = k;
+                else order[base_order + pos] = k;
+            }
+            if (threadIdx.x == 1023) s_total = sh[1023];
+            __syncthreads();
+            base += s_total;
+            __syncthreads();
+        }
+        if (cls < 2) {
+            const int groups = (base + 31) / 32;
+            for (int i = base + threadIdx.x; i < groups * 32; i += blockDim.x) order[base_order + i] = -1;
+            if (threadIdx.x == 0) counts[cls] = groups;
+            base_order += groups * 32;
+        } else {
+            nexact = base;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) counts[2] = nexact;
+}
+
+cudaError_t launch_angle_lists(const ProbGeom &P, int *order, int *exact, int *counts, cudaStream_t stream) {
+    angle_lists_kernel<<<1, 1024, 0, stream>>>(P.geom, P.a, order, exact, counts);
+    return cudaGetLastError();
+}
+
+// xpad[z][r][c+1] = x[z][r][c], xTpad[z][c][r+1] = x[z][r][c] (row stride N+2;
+// the pad columns are zeroed by the caller).
+__global__ void pad_kernel(const float *__restrict__ x, float *__restrict__ xpad, float *__restrict__ xTpad, int N) {
     __shared__ float tile[32][33];
     const size_t off = (size_t)blockIdx.z * N * N;
+    const size_t offp = (size_t)blockIdx.z * N * (N + 2);
     const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
     for (int y = threadIdx.y; y < 32; y += 8) {
         const int r = by + y, c = bx + threadIdx.x;
-        if (r < N && c < N) tile[y][threadIdx.x] = in[off + (size_t)r * N + c];
+        if (r < N && c < N) {
+            const float v = x[off + (size_t)r * N + c];
+            tile[y][threadIdx.x] = v;
+            xpad[offp + (size_t)r * (N + 2) + c + 1] = v;
+        }
     }
     __syncthreads();
     for (int y = threadIdx.y; y < 32; y += 8) {
         const int c = bx + y, r = by + threadIdx.x;
-        if (r < N && c < N) out[off + (size_t)c * N + r] = tile[threadIdx.x][y];
+        if (r < N && c < N) xTpad[offp + (size_t)c * (N + 2) + r + 1] = tile[threadIdx.x][y];
     }
 }
 
-cudaError_t launch_transpose(const float *in, float *out, int N, int nslices, cudaStream_t stream) {
+cudaError_t launch_pad(const float *x, float *xpad, float *xTpad, int N, int nslices, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(xpad, 0, sizeof(float) * (size_t)nslices * N * (N + 2), stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(xTpad, 0, sizeof(float) * (size_t)nslices * N * (N + 2), stream);
+    if (e != cudaSuccess) return e;
     dim3 grid((N + 31) / 32, (N + 31) / 32, nslices);
-    transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(in, out, N);
+    pad_kernel<<<grid, dim3(32, 8), 0, stream>>>(x, xpad, xTpad, N);
     return cudaGetLastError();
 }
 
-// Forward projection: ONES=false writes the ray sums, ONES=true writes the
-// normaliser R = safe_inverse(A*1) (SIRT.fut:22-23, sirtlib.fut:9-13).
-template <bool ONES>
-__global__ void __launch_bounds__(256) fp_kernel(ProbGeom P, const float *__restrict__ img,
-                                                 const float *__restrict__ imgT, float *__restrict__ out) {
+__global__ void unpad_kernel(const float *__restrict__ xpad, float *__restrict__ x, int N) {
+    const size_t z = blockIdx.z;
+    const int r = blockIdx.y;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x)
+        x[z * N * N + (size_t)r * N + c] = xpad[z * N * (N + 2) + (size_t)r * (N + 2) + c + 1];
+}
+
+cudaError_t launch_unpad(const float *xpad, float *x, int N, int nslices, cudaStream_t stream) {
+    dim3 grid((N + 255) / 256, N, nslices);
+    unpad_kernel<<<grid, 256, 0, stream>>>(xpad, x, N);
+    return cudaGetLastError();
+}
+
+// ---- forward projection ---------------------------------------------------------
+
+__global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
+                                                      const float *__restrict__ xTpad, float *__restrict__ sino) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = blockIdx.y;
+    const int nsteep = __ldg(L.counts), nflat = __ldg(L.counts + 1);
+    if (grp >= nsteep + nflat) return;              // block-uniform
+    const int r = blockIdx.x * 8 + warp;
+    if (r >= P.D) return;                           // warp-uniform
+    const int k = __ldg(L.order + grp * 32 + lane);
+    const float v = fp_lane_ray(P, k, r, grp < nsteep ? xpad : xTpad, 0, P.N);
+    if (k >= 0) sino[(size_t)k * P.D + r] = v;
+}
+
+__global__ void __launch_bounds__(128) fp_exact_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
+                                                       const float *__restrict__ xTpad, float *__restrict__ sino) {
+    const int nexact = __ldg(L.counts + 2);
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P.D) return;
+    for (int e = blockIdx.y; e < nexact; e += gridDim.y) {
+        const int k = __ldg(L.exact + e);
+        sino[(size_t)k * P.D + r] = fp_exact_ray(P, k, r, xpad, xTpad);
+    }
+}
+
+cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad, const float *xTpad, float *sino,
+                      cudaStream_t stream) {
+    dim3 grid((P.D + 7) / 8, (P.a + 31) / 32 + 2);
+    fp_lane_kernel<<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 ge((P.D + 127) / 128, 8);
+    fp_exact_kernel<<<ge, 128, 0, stream>>>(P, L, xpad, xTpad, sino);
+    return cudaGetLastError();
+}
+
+// ---- backprojection ---------------------------------------------------------------
+
+template <bool UNIT>
+__global__ void __launch_bounds__(256) bp_tile_kernel(ProbGeom P, AngleLists L, const float *__restrict__ sino,
+                                                      float *__restrict__ out) {
+    __shared__ BpStage st;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int col = blockIdx.x * 32 + lane;
+    const int row0 = blockIdx.y * 32 + warp;
+    const float xc = (float)(col - P.half) + 0.5f;
+    const float yc0 = (float)(row0 - P.half) + 0.5f;
+    float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f}, comp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int kc = 0; kc < P.a; kc += kBpChunk) {
+        __syncthreads();
+        bp_stage(P, kc, st);
+        __syncthreads();
+        float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        bp_chunk<4, UNIT>(P, st, kc, P.a, 0, 1, sino, xc, yc0, 8.0f, part);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], part[m]);
+    }
+    float ex[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    bp_exact_angles<4>(P, L.exact, __ldg(L.counts + 2), 0, 1, sino, row0, 8, col, ex);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int row = row0 + 8 * m;
+        if (row < P.N && col < P.N) out[(size_t)row * P.N + col] = (sum[m] + comp[m]) + ex[m];
+    }
+}
+
+cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream) {
+    dim3 grid((P.N + 31) / 32, (P.N + 31) / 32);
+    if (P.deltarho == 1.0f) bp_tile_kernel<true><<<grid, 256, 0, stream>>>(P, L, sino, img);
+    else bp_tile_kernel<false><<<grid, 256, 0, stream>>>(P, L, sino, img);
+    return cudaGetLastError();
+}
+
+// ---- normalisers (FP64 sums) -----------------------------------------------------------
+
+// R = safe_inverse(A*1): one thread per ray (SIRT.fut:22-23, sirtlib.fut:9-13).
+__global__ void __launch_bounds__(256) rownorm_kernel(ProbGeom P, float *__restrict__ R) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k = blockIdx.y * 8 + warp;
     const int r = blockIdx.x * 32 + lane;
     if (k >= P.a || r >= P.D) return;
     const AngleGeom g = load_geom(P.geom, k);
-    const float *frame = g.flat ? imgT : img;
-    const auto v = fp_ray<ONES>(P, g, frame, r, 0, P.N);
-    if constexpr (ONES) out[(size_t)k * P.D + r] = v != 0.0 ? (float)(1.0 / v) : 0.0f;
-    else out[(size_t)k * P.D + r] = v;
+    const double v = fp_ray<true>(P, g, nullptr, r, 0, P.N);
+    R[(size_t)k * P.D + r] = v != 0.0 ? (float)(1.0 / v) : 0.0f;
 }
 
-cudaError_t launch_fp(const ProbGeom &P, const float *img, const float *imgT, float *sino, cudaStream_t stream) {
-    dim3 grid((P.D + 31) / 32, (P.a + 7) / 8);
-    fp_kernel<false><<<grid, 256, 0, stream>>>(P, img, imgT, sino);
-    return cudaGetLastError();
-}
-
-// Backprojection: ONES=false writes the image, ONES=true writes the normaliser
-// C = safe_inverse(A^T*1) (SIRT.fut:25) with the angle sum in FP64.
-template <bool ONES>
-__global__ void __launch_bounds__(256) bp_kernel(ProbGeom P, const float *__restrict__ sino, float *__restrict__ out) {
+// C = safe_inverse(A^T*1): one thread per pixel, FP64 angle sum (SIRT.fut:25).
+__global__ void __launch_bounds__(256) colnorm_kernel(ProbGeom P, float *__restrict__ C) {
     const int col = blockIdx.x * 32 + (threadIdx.x & 31);
     const int row = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (row >= P.N || col >= P.N) return;
-    float sum = 0.0f, comp = 0.0f;
     double dsum = 0.0;
     for (int k0 = 0; k0 < P.a; k0 += 32) {
         const int k1 = min(k0 + 32, P.a);
         float part = 0.0f;
-        for (int k = k0; k < k1; ++k) {
-            const AngleGeom g = load_geom(P.geom, k);
-            part += bp_angle<ONES>(P, g, sino + (size_t)k * P.D, row, col);
-        }
-        if constexpr (ONES) dsum += (double)part;
-        else comp_add(sum, comp, part);
+        for (int k = k0; k < k1; ++k) part += bp_angle<true>(P, load_geom(P.geom, k), nullptr, row, col);
+        dsum += (double)part;
     }
-    if constexpr (ONES) out[(size_t)row * P.N + col] = dsum != 0.0 ? (float)(1.0 / dsum) : 0.0f;
-    else out[(size_t)row * P.N + col] = sum + comp;
-}
-
-cudaError_t launch_bp(const ProbGeom &P, const float *sino, float *img, cudaStream_t stream) {
-    dim3 grid((P.N + 31) / 32, (P.N + 7) / 8);
-    bp_kernel<false><<<grid, 256, 0, stream>>>(P, sino, img);
-    return cudaGetLastError();
+    C[(size_t)row * P.N + col] = dsum != 0.0 ? (float)(1.0 / dsum) : 0.0f;
 }
 
 cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, cudaStream_t stream) {
     dim3 gf((P.D + 31) / 32, (P.a + 7) / 8);
-    fp_kernel<true><<<gf, 256, 0, stream>>>(P, nullptr, nullptr, R);
+    rownorm_kernel<<<gf, 256, 0, stream>>>(P, R);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     dim3 gb((P.N + 31) / 32, (P.N + 7) / 8);
-    bp_kernel<true><<<gb, 256, 0, stream>>>(P, nullptr, C);
+    colnorm_kernel<<<gb, 256, 0, stream>>>(P, C);
     return cudaGetLastError();
 }
 

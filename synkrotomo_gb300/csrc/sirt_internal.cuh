@@ -2,6 +2,7 @@
 #pragma once
 
 #include "synk_internal.cuh"
+#include "fp_tile.cuh"
 
 namespace synk {
 
@@ -9,15 +10,15 @@ struct SirtParams {
     ProbGeom P;
     const float *R;       // [a*D] row normaliser (shared by all slices)
     const float *C;       // [N*N] column normaliser
+    AngleLists L;         // angle order of the lane-per-angle projector
     const float *b;       // [nslices][a*D] sinograms
-    float *x;             // [nslices][N*N] iterate (in: start, out: result)
-    float *xT;            // [nslices][N*N] transposed iterate
+    float *xpad;          // [nslices][N][N+2] iterate, zero column on each side
+    float *xTpad;         // [nslices][N][N+2] transposed iterate, same padding
     float *rr;            // [nslices][a*D] weighted residual R*(b - FP(x))
     double *res2;         // [nslices][iterations+1] sum of (b - FP(x_k))^2
     const double *b2;     // [nslices] ||b||^2
     int *stop_iter;       // [nslices] iteration at which the stopping rule fired (init: iterations)
     unsigned *bar;        // [2] barrier arrival count and generation
-    unsigned *work;       // [3] rotating work counters
     int *status;          // SYNK_OK or SYNK_ETIMEOUT
     unsigned long long timeout_ns;
     double tol2;          // relative tolerance squared (0: no stopping rule)

@@ -84,6 +84,21 @@ struct ProbGeom {
     const AngleGeom *geom;   // [a]
 };
 
+// Left end of a fast-path ray's segment in frame row 0, in pixel-index units:
+// u0 = intercept + min(slope,0) + half - half*slope.  Every kernel that walks a
+// ray (projectors, SIRT, CSR builders) uses this one expression with explicit
+// rounding, so all of them see bit-identical segments.
+__device__ __forceinline__ float ray_u0(const ProbGeom &P, const AngleGeom &g, float intercept) {
+    const float halff = (float)P.half;
+    return __fmaf_rn(-halff, g.slope, __fadd_rn(__fadd_rn(intercept, g.slope_lo), halff));
+}
+
+// Share of the right pixel c+1 of a row segment whose left end is u, with
+// fl = floor(u): (u - fl + |slope| - 1) / |slope| clamped to [0, 1].
+__device__ __forceinline__ float right_share(float u, float fl, float ainv) {
+    return __saturatef(__fmaf_rn(__fsub_rn(u, fl), ainv, __fsub_rn(1.0f, ainv)));
+}
+
 // ---------------------------------------------------------------------------
 // Forward projection of one ray: sum over the rows of the traversal frame.
 // img points at the image seen in that frame (the transposed image for flat
@@ -100,7 +115,6 @@ template <bool ONES>
 __device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int N, float slope, float u0,
                                              float ainv, int j0, int j1,
                                              typename FpAcc<ONES>::T &sum, float &comp) {
-    const float bias = 1.0f - ainv;
     const unsigned uN = (unsigned)N;
     int j = j0;
     while (j < j1) {
@@ -113,7 +127,7 @@ __device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int 
             const float u = fmaf((float)j, slope, u0);
             int c;
             const float fl = floor_magic(u, c);
-            const float t = fmaxf(fmaf(__fsub_rn(u, fl), ainv, bias), 0.0f);  // share of pixel c+1
+            const float t = right_share(u, fl, ainv);                      // share of pixel c+1
             float v0, v1;
             if constexpr (ONES) {
                 v0 = ((unsigned)c < uN) ? 1.0f : 0.0f;
@@ -131,11 +145,12 @@ __device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int 
 
 // The reference's own expressions (forwardprojection.fut:31-56), used for
 // near-axis lines: every operation rounds exactly as the f32 reference.
+// img points at pixel (0, 0) of the frame, rows `stride` floats apart.
 template <bool ONES>
-__device__ __forceinline__ void fp_rows_exact(const float *__restrict__ img, int N, int half, float slope,
+__device__ __forceinline__ void fp_rows_exact(const float *__restrict__ img, int stride, int half, float slope,
                                               float intercept, float lbase,
                                               typename FpAcc<ONES>::T &sum) {
-    const int size = N;
+    const int size = stride;
     typename FpAcc<ONES>::T acc = 0;
     for (int i = -half; i < half; ++i) {
         const float xbot = __fadd_rn(__fmul_rn((float)i, slope), intercept);
@@ -179,12 +194,11 @@ __device__ __forceinline__ typename FpAcc<ONES>::T fp_ray(const ProbGeom &P, con
         // whole ray in one piece (only the row-part starting at 0 computes it)
         if (jbeg != 0) return (T)0;
         T s;
-        fp_rows_exact<ONES>(img_frame, P.N, P.half, g.slope, intercept, g.lbase, s);
+        fp_rows_exact<ONES>(img_frame, P.N, P.half, g.slope, intercept, g.lbase, s);   // unpadded frame
         return s;
     }
     // u(j) = xlo(row j) + half, xlo = xbot + min(slope,0), xbot = (j-half)*slope + intercept
-    const float halff = (float)P.half;
-    const float u0 = intercept + g.slope_lo + halff - halff * g.slope;
+    const float u0 = ray_u0(P, g, intercept);
     // rows where the segment [u, u+|slope|] can touch a pixel column in [0, N)
     const float aslope = fabsf(g.slope);
     int j0 = jbeg, j1 = jend;
@@ -274,10 +288,11 @@ __device__ __forceinline__ AngleGeom load_geom(const AngleGeom *__restrict__ gt,
 // ---------------------------------------------------------------------------
 // Kernel launchers implemented in the .cu files (all enqueue on `stream`).
 // ---------------------------------------------------------------------------
+struct AngleLists;
 cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStream_t stream);
-cudaError_t launch_transpose(const float *in, float *out, int N, int nslices, cudaStream_t stream);
-cudaError_t launch_fp(const ProbGeom &P, const float *img, const float *imgT, float *sino, cudaStream_t stream);
-cudaError_t launch_bp(const ProbGeom &P, const float *sino, float *img, cudaStream_t stream);
+cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad, const float *xTpad, float *sino,
+                      cudaStream_t stream);
+cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream);
 cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, cudaStream_t stream);
 
 }  // namespace synk

@@ -261,3 +261,65 @@ def sirt3d(angles: torch.Tensor, rhos: torch.Tensor, projections: torch.Tensor, 
 def image_side(n: int) -> int:
     s = math.isqrt(int(n))
     return s
+
+
+class SystemMatrix:
+    """The forward projector's rule as a CSR matrix A (rays x pixels) and its
+    exact transpose, built and held on the GPU (``synk_csr_*`` of the C ABI)."""
+
+    def __init__(self, angles: torch.Tensor, rhozero: float, deltarho: float, numrhos: int, size: int):
+        self._ctx = context(angles.device.index)
+        self.device = angles.device
+        h = ctypes.c_void_p()
+        rc = self._ctx.lib.synk_csr_new(self._ctx.handle, ctypes.byref(h), _ptr(angles), angles.numel(),
+                                        float(rhozero), float(deltarho), int(numrhos), int(size))
+        self._ctx.check(rc, "synk_csr_new")
+        self._h = h
+        r, c, z = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._ctx.lib.synk_csr_shape(h, ctypes.byref(r), ctypes.byref(c), ctypes.byref(z))
+        self.rows, self.cols, self.nnz = r.value, c.value, z.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._ctx.lib.synk_csr_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def matvec(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        ctx = context(self.device.index)
+        if out is None:
+            out = torch.empty(self.rows, dtype=torch.float32, device=self.device)
+        ctx.check(ctx.lib.synk_csr_spmv(ctx.handle, self._h, _ptr(x), _ptr(out)), "synk_csr_spmv")
+        return out
+
+    def rmatvec(self, y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        ctx = context(self.device.index)
+        if out is None:
+            out = torch.empty(self.cols, dtype=torch.float32, device=self.device)
+        ctx.check(ctx.lib.synk_csr_spmv_t(ctx.handle, self._h, _ptr(y), _ptr(out)), "synk_csr_spmv_t")
+        return out
+
+    def arrays(self, transpose: bool = False):
+        """(rowptr int64, colidx int32, vals float32) of A or A^T as device tensors (views)."""
+        p, i, v = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        self._ctx.lib.synk_csr_arrays(self._h, int(transpose), ctypes.byref(p), ctypes.byref(i), ctypes.byref(v))
+        n = self.cols if transpose else self.rows
+        return (device_view(p.value, n + 1, "<i8", self.device), device_view(i.value, self.nnz, "<i4", self.device),
+                device_view(v.value, self.nnz, "<f4", self.device))
+
+
+class _CudaArray:
+    def __init__(self, ptr: int, n: int, typestr: str):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def device_view(ptr: int, n: int, typestr: str, device) -> torch.Tensor:
+    """A torch tensor viewing ``n`` elements of library-owned device memory."""
+    if n == 0:
+        dt = {"<i8": torch.int64, "<i4": torch.int32, "<f4": torch.float32}[typestr]
+        return torch.empty(0, dtype=dt, device=device)
+    return torch.as_tensor(_CudaArray(ptr, n, typestr), device=device)
