@@ -148,6 +148,22 @@ int synk_csr_spmv_t(synk_context *ctx, const synk_csr *m, const float *y, float 
 int synk_spmv_csr32(synk_context *ctx, int64_t rows, const int32_t *rowptr, const int32_t *colidx,
                     const float *vals, const float *x, float *y);
 
+/* ---- backprojection that allocates nothing (no counterpart in the reference) ----
+ * For callers that cannot let the library allocate device memory: programs
+ * that reserve all free device memory for their own allocator at start-up,
+ * and acquisition loops that must not enter the CUDA allocator while frames
+ * stream (an allocation can take the driver's allocator lock or synchronise
+ * the device).  Same arguments and result as synk_backprojection, at most
+ * SYNK_NOALLOC_MAX_ANGLES angles (larger counts return SYNK_EINVAL).  Its
+ * scratch is one file-scope device array (about 448 KiB) that every GPU
+ * loading the library holds until exit.  The first call on a device looks up
+ * that array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+#define SYNK_NOALLOC_MAX_ANGLES 8192
+int synk_backprojection_noalloc(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
+                                float deltarho, int32_t size, const float *projections, int64_t p);
+
 #ifdef __cplusplus
 }
 #endif

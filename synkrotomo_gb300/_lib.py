@@ -74,6 +74,9 @@ SIGNATURES = {
     "synk_csr_spmv_t": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "synk_spmv_csr32": (ctypes.c_int, [c_ctx, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p]),
+    "synk_backprojection_noalloc": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                                   ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_void_p,
+                                                   ctypes.c_int64]),
 }
 
 

@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -542,3 +543,84 @@ int synk_spmv_csr32(synk_context *ctx, int64_t rows, const int32_t *rowptr, cons
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Backprojection without any allocation.
+//
+// Some callers of this library cannot let it allocate device memory: programs
+// that reserve all free device memory for their own allocator at start-up (a
+// library cudaMalloc/cudaMallocAsync then fails or fragments their pool), and
+// acquisition loops that must never enter the CUDA allocator while frames are
+// streaming, because an allocation can take the driver's allocator lock or
+// synchronise the device and stall a running stream.
+//
+// synk_backprojection_noalloc is synk_backprojection with its scratch (the
+// per-angle geometry table and the angle lists) kept in one file-scope
+// __device__ array instead of stream-ordered allocations.  The array is sized
+// for at most SYNK_NOALLOC_MAX_ANGLES angles (about 448 KiB) and every GPU on
+// which the library is loaded holds it until the process exits.  Every call
+// shares the array and overwrites it completely before reading it (nothing in
+// it has to start at zero), so calls that overlap on the GPU -- on two streams,
+// or from two host threads -- race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct NoAllocScratch {
+    AngleGeom geom[SYNK_NOALLOC_MAX_ANGLES];
+    int order[SYNK_NOALLOC_MAX_ANGLES + 64];
+    int exact[SYNK_NOALLOC_MAX_ANGLES];
+    int counts[4];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+constexpr int kMaxDevices = 256;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (set-up once per
+// device; the host-side symbol itself is not a device address).
+int noalloc_scratch(synk_context *ctx, NoAllocScratch **out) {
+    if (ctx->device < 0 || ctx->device >= kMaxDevices) return fail(ctx, SYNK_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[ctx->device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return cuda_fail(ctx, e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                                                     "cudaGetSymbolAddress(no-allocation scratch)");
+        g_noalloc_addr[ctx->device] = p;
+    }
+    *out = static_cast<NoAllocScratch *>(g_noalloc_addr[ctx->device]);
+    return SYNK_OK;
+}
+
+}  // namespace
+
+extern "C" int synk_backprojection_noalloc(synk_context *ctx, float *out, const float *angles, int64_t a,
+                                           float rhozero, float deltarho, int32_t size, const float *projections,
+                                           int64_t p) {
+    int rc = check_ctx(ctx);   // makes the context's device current
+    if (rc) return rc;
+    if (!out || !angles || !projections) return fail(ctx, SYNK_EINVAL, "null array pointer");
+    if (a < 1) return fail(ctx, SYNK_EINVAL, "need at least one angle (got %lld)", (long long)a);
+    if (a > SYNK_NOALLOC_MAX_ANGLES)
+        return fail(ctx, SYNK_EINVAL, "synk_backprojection_noalloc supports at most %d angles (got %lld); "
+                    "use synk_backprojection", SYNK_NOALLOC_MAX_ANGLES, (long long)a);
+    if (p < a || p % a) return fail(ctx, SYNK_EINVAL, "projection length %lld is not a multiple of %lld angles",
+                                    (long long)p, (long long)a);
+    const int64_t numrhos = p / a;
+    if ((rc = check_geometry(ctx, a, rhozero, deltarho, numrhos, size))) return rc;
+    NoAllocScratch *sc = nullptr;
+    if ((rc = noalloc_scratch(ctx, &sc))) return rc;
+    cudaStream_t st = ctx->stream;
+    SYNK_CUDA(launch_geometry(angles, (int)a, sc->geom, st), "geometry kernel");
+    const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size, sc->geom);
+    SYNK_CUDA(launch_angle_lists(P, sc->order, sc->exact, sc->counts, st), "angle lists kernel");
+    AngleLists L;
+    L.order = sc->order;
+    L.exact = sc->exact;
+    L.counts = sc->counts;
+    SYNK_CUDA(launch_bp(P, L, projections, out, st), "backprojection kernel");
+    return SYNK_OK;
+}
