@@ -256,8 +256,9 @@ def run_gpu(args, rank, world):
     # end to end through the public API, pinned host buffers
     e2e = run_e2e(args, g, img, sino, dev)
     sirt = run_sirt_cfg0(dev) if (rank == 0 and not args.skip_sirt) else None
+    csr = run_csr_cfg1(dev) if (rank == 0 and not args.skip_csr) else None
     return {"step_ms": step_ms, "fp_ms": statistics.median(fp_ms), "bp_ms": statistics.median(bp_ms),
-            "wall_s": wall, "clocks": clk.summary(), "e2e": e2e, "sirt": sirt,
+            "wall_s": wall, "clocks": clk.summary(), "e2e": e2e, "sirt": sirt, "csr": csr,
             "sms": torch.cuda.get_device_properties(dev).multi_processor_count}
 
 
@@ -328,6 +329,46 @@ def run_sirt_cfg0(dev):
     return out
 
 
+def run_csr_cfg1(dev, reps=20):
+    """CSR SpMV on the sparse projector configuration (N=512, 512 angles, 725
+    detectors): GB/s of the compulsory traffic 8*nnz + 4*(rows+1) + 4*cols +
+    4*rows per A*x (column vector gathered once) and the same for A^T*y."""
+    import torch
+
+    from synkrotomo_gb300 import phantom
+    from synkrotomo_gb300 import runtime as rt
+
+    g = phantom.geometry(512, 512, numrhos=725)
+    t0 = time.perf_counter()
+    m = rt.SystemMatrix(torch.from_numpy(g.angles).to(dev), g.rhozero, g.deltarho, g.numrhos, 512)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    x = torch.from_numpy(phantom.ellipse_phantom(512, 0)).to(dev)
+    y = torch.rand(m.rows, device=dev)
+    ax = torch.empty(m.rows, device=dev)
+    aty = torch.empty(m.cols, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
+    out = {"nnz": m.nnz, "rows": m.rows, "cols": m.cols, "build_s": build_s}
+    for name, fn, rows, cols in (("Ax", lambda: m.matvec(x, ax), m.rows, m.cols),
+                                 ("ATy", lambda: m.rmatvec(y, aty), m.cols, m.rows)):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(reps):
+            flush.fill_(0.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = statistics.median(ts)
+        nbytes = 8 * m.nnz + 8 * (rows + 1) + 4 * cols + 4 * rows   # int64 row pointers
+        out[name] = {"ms": ms, "GB/s": nbytes / (ms * 1e-3) / 1e9, "bytes": nbytes}
+    del m
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -336,6 +377,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-sirt", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-csr", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -409,6 +451,13 @@ def main():
                    "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["ms"]}
     if res["sirt"] is not None:
         line["sirt_cfg0"] = res["sirt"]
+    if res["csr"] is not None:
+        c = res["csr"]
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        for k in ("Ax", "ATy"):
+            c[k]["frac_hbm"] = c[k]["GB/s"] / hbm
+        c["hbm_peak_gbs"] = hbm
+        line["csr_cfg1"] = c
     if not args.skip_cpu:
         r = cpu_reference_rate(budget_s=10.0)
         cv = step_bytes() / r["step_s"] / 1e9

@@ -116,6 +116,8 @@ typedef struct synk_sirt_options {
     /* Rows (FP) / angles (BP) split per work item: 0 = automatic. */
     int32_t fp_split;
     int32_t bp_split;
+    /* Blocks of the persistent launch: 0 = every block that fits on the GPU. */
+    int32_t grid_blocks;
 } synk_sirt_options;
 
 /* SIRT of `nslices` independent slices sharing one geometry in ONE persistent
@@ -124,6 +126,39 @@ typedef struct synk_sirt_options {
 int synk_sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
                      float deltarho, int32_t numrhos, int32_t size, int32_t nslices, const float *image,
                      const float *projections, int32_t iterations, const synk_sirt_options *opts);
+
+/* Independent SIRT problems of any sizes in ONE persistent launch (no
+ * reference counterpart; SIRT3D is the special case of one problem with many
+ * slices).  Each problem is a stack of `nslices` slices sharing one geometry.
+ * All arrays are device pointers: image [nslices*size*size] (NULL = zero
+ * start), projections [nslices*a*numrhos], out [nslices*size*size],
+ * residuals (optional) [nslices][iterations+1], iterations_done (optional)
+ * [nslices]. */
+typedef struct synk_sirt_problem {
+    const float *angles;
+    int64_t a;
+    float rhozero;
+    float deltarho;
+    int32_t numrhos;
+    int32_t size;
+    int32_t nslices;
+    int32_t iterations;
+    const float *image;
+    const float *projections;
+    float *out;
+    double *residuals;
+    int32_t *iterations_done;
+    int32_t fp_split;   /* 0 = automatic */
+    int32_t bp_split;   /* 0 = automatic */
+} synk_sirt_problem;
+
+/* Blocks of the persistent SIRT kernel that fit on the current device at once
+ * (the largest useful grid_blocks); 0 if it cannot be resident. */
+int synk_sirt_resident_blocks(void);
+
+/* tol and grid_blocks as in synk_sirt_options. */
+int synk_sirt_batch(synk_context *ctx, int32_t nprob, const synk_sirt_problem *probs, double tol,
+                    int32_t grid_blocks);
 
 /* ---- CSR system matrix (no reference counterpart) ----
  * The forward projector's rule (futhark/forwardprojection.fut:31-56) stored

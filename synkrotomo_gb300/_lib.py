@@ -33,6 +33,29 @@ class SynkOptions(ctypes.Structure):
         ("iterations_done", ctypes.c_void_p),
         ("fp_split", ctypes.c_int32),
         ("bp_split", ctypes.c_int32),
+        ("grid_blocks", ctypes.c_int32),
+    ]
+
+
+class SynkProblem(ctypes.Structure):
+    """``synk_sirt_problem`` of include/synk.h."""
+
+    _fields_ = [
+        ("angles", ctypes.c_void_p),
+        ("a", ctypes.c_int64),
+        ("rhozero", ctypes.c_float),
+        ("deltarho", ctypes.c_float),
+        ("numrhos", ctypes.c_int32),
+        ("size", ctypes.c_int32),
+        ("nslices", ctypes.c_int32),
+        ("iterations", ctypes.c_int32),
+        ("image", ctypes.c_void_p),
+        ("projections", ctypes.c_void_p),
+        ("out", ctypes.c_void_p),
+        ("residuals", ctypes.c_void_p),
+        ("iterations_done", ctypes.c_void_p),
+        ("fp_split", ctypes.c_int32),
+        ("bp_split", ctypes.c_int32),
     ]
 
 
@@ -63,6 +86,9 @@ SIGNATURES = {
                                         ctypes.c_float, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                         ctypes.POINTER(SynkOptions)]),
+    "synk_sirt_resident_blocks": (ctypes.c_int, []),
+    "synk_sirt_batch": (ctypes.c_int, [c_ctx, ctypes.c_int32, ctypes.POINTER(SynkProblem), ctypes.c_double,
+                                       ctypes.c_int32]),
     "synk_csr_new": (ctypes.c_int, [c_ctx, ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.c_int64,
                                     ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_int32]),
     "synk_csr_free": (None, [ctypes.c_void_p]),

@@ -5,6 +5,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <climits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -210,93 +212,174 @@ __global__ void fill_i32_kernel(int *p, int n, int v) {
     if (i < n) p[i] = v;
 }
 
-int sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero, float deltarho,
-                int64_t numrhos, int64_t size, int64_t nslices, const float *image, const float *projections,
-                int32_t iterations, const synk_sirt_options *opts) {
+int pick_fp_split(long long tasks, long long resident_warps, int size) {
+    const int maxs = size / 16 > 8 ? 8 : (size / 16 < 1 ? 1 : size / 16);
+    return pick_split(tasks, resident_warps, maxs);
+}
+int pick_bp_split(long long tasks, long long resident_warps, int64_t a) {
+    const int maxs = a / 8 > 8 ? 8 : (a / 8 < 1 ? 1 : (int)(a / 8));
+    return pick_split(tasks, resident_warps, maxs);
+}
+
+int valid_split(int s) { return s == 1 || s == 2 || s == 4 || s == 8; }
+
+int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double tol, int grid_blocks) {
     int rc;
-    if (!out || !angles || !projections) return fail(ctx, SYNK_EINVAL, "null array pointer");
-    if ((rc = check_geometry(ctx, a, rhozero, deltarho, numrhos, size))) return rc;
-    if (nslices < 1 || nslices > (1 << 20)) return fail(ctx, SYNK_EINVAL, "bad slice count %lld", (long long)nslices);
-    if (iterations < 0) return fail(ctx, SYNK_EINVAL, "iterations must be >= 0 (got %d)", iterations);
-    const size_t n = (size_t)size * size, pr = (size_t)a * numrhos;
-    if ((double)nslices * (double)(n > pr ? n : pr) > 2.0e9 * 4)
-        return fail(ctx, SYNK_EINVAL, "slice stack too large");
+    if (nprob < 1 || nprob > (1 << 16)) return fail(ctx, SYNK_EINVAL, "bad problem count %d", nprob);
+    if (!in) return fail(ctx, SYNK_EINVAL, "null problem table");
+    if (!(tol >= 0.0) || !isfinite(tol)) return fail(ctx, SYNK_EINVAL, "tol must be finite and >= 0");
     cudaStream_t st = ctx->stream;
-    // start image
-    if (image) SYNK_CUDA(cudaMemcpyAsync(out, image, sizeof(float) * n * nslices, cudaMemcpyDeviceToDevice, st), "copy start");
-    else SYNK_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * n * nslices, st), "zero start");
-    if (iterations == 0 && !(opts && opts->residuals)) {
-        if (opts && opts->iterations_done) SYNK_CUDA(cudaMemsetAsync(opts->iterations_done, 0, sizeof(int) * nslices, st), "memset");
+    int bps = 0;
+    const int resident = sirt_persistent_grid(&bps);
+    if (resident < 1) return fail(ctx, SYNK_ECUDA, "persistent SIRT kernel cannot be resident");
+    int grid = resident;
+    if (grid_blocks > 0 && grid_blocks < grid) grid = grid_blocks;
+    const long long resident_warps = (long long)grid * 8;
+    int max_iter = 0, max_slices = 1;
+    bool any_work = false, want_res = false;
+    for (int i = 0; i < nprob; ++i) {
+        const synk_sirt_problem &q = in[i];
+        if (!q.out || !q.angles || !q.projections) return fail(ctx, SYNK_EINVAL, "problem %d: null array pointer", i);
+        if ((rc = check_geometry(ctx, q.a, q.rhozero, q.deltarho, q.numrhos, q.size))) return rc;
+        if (q.nslices < 1 || q.nslices > (1 << 20)) return fail(ctx, SYNK_EINVAL, "problem %d: bad slice count %d", i, q.nslices);
+        if (q.iterations < 0) return fail(ctx, SYNK_EINVAL, "iterations must be >= 0 (got %d)", q.iterations);
+        if ((q.fp_split && !valid_split(q.fp_split)) || (q.bp_split && !valid_split(q.bp_split)))
+            return fail(ctx, SYNK_EINVAL, "problem %d: work splits must be 0, 1, 2, 4 or 8", i);
+        const size_t n = (size_t)q.size * q.size, pr = (size_t)q.a * q.numrhos;
+        if ((double)q.nslices * (double)(n > pr ? n : pr) > 8.0e9)
+            return fail(ctx, SYNK_EINVAL, "problem %d: slice stack too large", i);
+        max_iter = q.iterations > max_iter ? q.iterations : max_iter;
+        max_slices = q.nslices > max_slices ? q.nslices : max_slices;
+        if (q.iterations > 0) any_work = true;
+        if (q.residuals) want_res = true;
+    }
+    // start images
+    for (int i = 0; i < nprob; ++i) {
+        const synk_sirt_problem &q = in[i];
+        const size_t bytes = sizeof(float) * (size_t)q.size * q.size * q.nslices;
+        if (q.image) SYNK_CUDA(cudaMemcpyAsync(q.out, q.image, bytes, cudaMemcpyDeviceToDevice, st), "copy start");
+        else SYNK_CUDA(cudaMemsetAsync(q.out, 0, bytes, st), "zero start");
+    }
+    if (!any_work && !want_res) {
+        for (int i = 0; i < nprob; ++i)
+            if (in[i].iterations_done)
+                SYNK_CUDA(cudaMemsetAsync(in[i].iterations_done, 0, sizeof(int) * in[i].nslices, st), "memset");
         return SYNK_OK;
     }
     Scratch sc(st);
-    AngleGeom *geom;
-    float *R, *C, *xpad, *xTpad, *rr;
-    double *res2, *b2;
-    int *stop_iter;
+    std::vector<SirtProblem> host(nprob);
+    for (int i = 0; i < nprob; ++i) {
+        const synk_sirt_problem &q = in[i];
+        SirtProblem &h = host[i];
+        const size_t n = (size_t)q.size * q.size, pr = (size_t)q.a * q.numrhos;
+        const size_t np = (size_t)q.size * (q.size + 2), K = (size_t)q.iterations + 1;
+        AngleGeom *geom;
+        float *R, *C, *xpad, *xTpad, *rr;
+        double *res2, *b2;
+        int *stop_iter;
+        SYNK_CUDA(sc.get(&geom, (size_t)q.a), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&R, pr), "cudaMallocAsync(R)");
+        SYNK_CUDA(sc.get(&C, n), "cudaMallocAsync(C)");
+        SYNK_CUDA(sc.get(&xpad, np * q.nslices), "cudaMallocAsync(padded image)");
+        SYNK_CUDA(sc.get(&xTpad, np * q.nslices), "cudaMallocAsync(padded transposed image)");
+        SYNK_CUDA(sc.get(&rr, pr * q.nslices), "cudaMallocAsync(residual)");
+        SYNK_CUDA(sc.get(&res2, K * q.nslices), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&b2, (size_t)q.nslices), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&stop_iter, (size_t)q.nslices), "cudaMallocAsync");
+        SYNK_CUDA(cudaMemsetAsync(res2, 0, sizeof(double) * K * q.nslices, st), "memset");
+        SYNK_CUDA(cudaMemsetAsync(b2, 0, sizeof(double) * q.nslices, st), "memset");
+        fill_i32_kernel<<<(unsigned)((q.nslices + 255) / 256), 256, 0, st>>>(stop_iter, q.nslices, INT_MAX);
+        SYNK_CUDA(cudaGetLastError(), "fill kernel");
+        SYNK_CUDA(launch_geometry(q.angles, (int)q.a, geom, st), "geometry kernel");
+        h.P = make_geom(q.a, q.rhozero, q.deltarho, q.numrhos, q.size, geom);
+        SYNK_CUDA(make_lists(sc, h.P, &h.L, st), "angle lists");
+        SYNK_CUDA(launch_normalisers(h.P, R, C, st), "normaliser kernels");
+        SYNK_CUDA(launch_pad(q.out, xpad, xTpad, q.size, q.nslices, st), "pad kernel");
+        SYNK_CUDA(launch_sumsq(q.projections, pr, q.nslices, b2, st), "norm kernel");
+        h.R = R;
+        h.C = C;
+        h.b = q.projections;
+        h.xpad = xpad;
+        h.xTpad = xTpad;
+        h.rr = rr;
+        h.res2 = res2;
+        h.b2 = b2;
+        h.stop_iter = stop_iter;
+        h.residuals = q.residuals;
+        h.iters_done = q.iterations_done;
+        h.nslices = q.nslices;
+        h.iterations = q.iterations;
+        // warp tasks per phase: one detector x 32 angles (FP), one 32-column x 4-row strip (BP)
+        const long long fp_tasks = (long long)q.nslices * q.numrhos * ((q.a + 31) / 32);
+        const long long bp_tasks = (long long)q.nslices * ((q.size + 3) / 4) * ((q.size + 31) / 32);
+        const long long share = nprob > 1 ? resident_warps / nprob + 1 : resident_warps;
+        h.fp_split = q.fp_split ? q.fp_split : pick_fp_split(fp_tasks, share, q.size);
+        h.bp_split = q.bp_split ? q.bp_split : pick_bp_split(bp_tasks, share, q.a);
+        h.fp_ips = h.bp_ips = 0;
+        h.fp_begin = h.bp_begin = 0;
+    }
+    // largest problems first: with the atomic hand-out the long items start early
+    std::vector<int> order(nprob);
+    for (int i = 0; i < nprob; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const double cx = (double)in[x].size * in[x].size * in[x].a * in[x].nslices;
+        const double cy = (double)in[y].size * in[y].size * in[y].a * in[y].nslices;
+        return cx > cy;
+    });
+    std::vector<SirtProblem> sorted(nprob);
+    for (int i = 0; i < nprob; ++i) sorted[i] = host[order[i]];
+    SirtProblem *dprobs;
+    long long *totals;
     unsigned *words;
-    const size_t K = (size_t)iterations + 1;
-    const size_t np = (size_t)size * (size + 2);
-    SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync");
-    SYNK_CUDA(sc.get(&R, pr), "cudaMallocAsync(R)");
-    SYNK_CUDA(sc.get(&C, n), "cudaMallocAsync(C)");
-    SYNK_CUDA(sc.get(&xpad, np * nslices), "cudaMallocAsync(padded image)");
-    SYNK_CUDA(sc.get(&xTpad, np * nslices), "cudaMallocAsync(padded transposed image)");
-    SYNK_CUDA(sc.get(&rr, pr * nslices), "cudaMallocAsync(residual)");
-    SYNK_CUDA(sc.get(&res2, K * nslices), "cudaMallocAsync");
-    SYNK_CUDA(sc.get(&b2, (size_t)nslices), "cudaMallocAsync");
-    SYNK_CUDA(sc.get(&stop_iter, (size_t)nslices), "cudaMallocAsync");
+    SYNK_CUDA(sc.get(&dprobs, (size_t)nprob), "cudaMallocAsync(problem table)");
+    SYNK_CUDA(sc.get(&totals, 2), "cudaMallocAsync");
     SYNK_CUDA(sc.get(&words, 8), "cudaMallocAsync");
-    SYNK_CUDA(cudaMemsetAsync(res2, 0, sizeof(double) * K * nslices, st), "memset");
-    SYNK_CUDA(cudaMemsetAsync(b2, 0, sizeof(double) * nslices, st), "memset");
+    // from pageable memory: the copy is staged before the call returns, so the
+    // host vector may go out of scope afterwards
+    SYNK_CUDA(cudaMemcpyAsync(dprobs, sorted.data(), sizeof(SirtProblem) * nprob, cudaMemcpyHostToDevice, st),
+              "upload problem table");
     SYNK_CUDA(cudaMemsetAsync(words, 0, sizeof(unsigned) * 8, st), "memset");
-    fill_i32_kernel<<<(unsigned)((nslices + 255) / 256), 256, 0, st>>>(stop_iter, (int)nslices, 0x7fffffff);
-    SYNK_CUDA(cudaGetLastError(), "fill kernel");
-    SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
-    const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size, geom);
-    AngleLists L;
-    SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
-    SYNK_CUDA(launch_normalisers(P, R, C, st), "normaliser kernels");
-    SYNK_CUDA(launch_pad(out, xpad, xTpad, (int)size, (int)nslices, st), "pad kernel");
-    SYNK_CUDA(launch_sumsq(projections, pr, (int)nslices, b2, st), "norm kernel");
-
+    SYNK_CUDA(launch_sirt_plan(dprobs, nprob, totals, st), "plan kernel");
     SirtParams sp;
-    sp.P = P;
-    sp.R = R;
-    sp.C = C;
-    sp.L = L;
-    sp.b = projections;
-    sp.xpad = xpad;
-    sp.xTpad = xTpad;
-    sp.rr = rr;
-    sp.res2 = res2;
-    sp.b2 = b2;
-    sp.stop_iter = stop_iter;
+    sp.probs = dprobs;
+    sp.totals = totals;
+    sp.nprob = nprob;
+    sp.max_iterations = max_iter;
     sp.bar = words;
+    sp.work = words + 4;
     sp.status = ctx->d_status;
     sp.timeout_ns = ctx->barrier_timeout_ns;
-    sp.tol2 = (opts && opts->tol > 0.0) ? opts->tol * opts->tol : 0.0;
-    sp.nslices = (int)nslices;
-    sp.iterations = iterations;
-    sp.record_final = (opts && opts->residuals) ? 1 : 0;
-    int bps = 0;
-    const int grid = sirt_persistent_grid(&bps);
-    if (grid < 1) return fail(ctx, SYNK_ECUDA, "persistent SIRT kernel cannot be resident");
-    const long long resident_warps = (long long)grid * 8;
-    // warp tasks per phase: one detector x 32 angles (FP), one 32-column x 4-row strip (BP)
-    const long long fp_tasks = (long long)nslices * numrhos * ((a + 31) / 32);
-    const long long bp_tasks = (long long)nslices * ((size + 3) / 4) * ((size + 31) / 32);
-    int fs = opts && opts->fp_split > 0 ? opts->fp_split : pick_split(fp_tasks, resident_warps, (int)(size / 16 > 8 ? 8 : (size / 16 < 1 ? 1 : size / 16)));
-    int bs = opts && opts->bp_split > 0 ? opts->bp_split : pick_split(bp_tasks, resident_warps, (int)(a / 8 > 8 ? 8 : (a / 8 < 1 ? 1 : a / 8)));
-    if (fs != 1 && fs != 2 && fs != 4 && fs != 8) return fail(ctx, SYNK_EINVAL, "fp_split must be 1, 2, 4 or 8");
-    if (bs != 1 && bs != 2 && bs != 4 && bs != 8) return fail(ctx, SYNK_EINVAL, "bp_split must be 1, 2, 4 or 8");
-    sp.fp_split = fs;
-    sp.bp_split = bs;
+    sp.tol2 = tol > 0.0 ? tol * tol : 0.0;
+    sp.record_final = want_res ? 1 : 0;
+    sp.dynamic = nprob > 1 ? 1 : 0;
     SYNK_CUDA(launch_sirt_persistent(sp, grid, st), "persistent SIRT kernel");
-    SYNK_CUDA(launch_unpad(xpad, out, (int)size, (int)nslices, st), "unpad kernel");
-    if (opts && (opts->residuals || opts->iterations_done))
-        SYNK_CUDA(launch_sirt_finalize(sp, opts->residuals, opts->iterations_done, st), "finalize kernel");
+    for (int i = 0; i < nprob; ++i)
+        SYNK_CUDA(launch_unpad(host[i].xpad, in[i].out, in[i].size, in[i].nslices, st), "unpad kernel");
+    SYNK_CUDA(launch_sirt_finalize(dprobs, nprob, max_slices, sp.record_final, st), "finalize kernel");
     return SYNK_OK;
+}
+
+int sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero, float deltarho,
+                int64_t numrhos, int64_t size, int64_t nslices, const float *image, const float *projections,
+                int32_t iterations, const synk_sirt_options *opts) {
+    synk_sirt_problem q = {};
+    q.angles = angles;
+    q.a = a;
+    q.rhozero = rhozero;
+    q.deltarho = deltarho;
+    q.numrhos = (int32_t)numrhos;
+    q.size = (int32_t)size;
+    q.nslices = (int32_t)nslices;
+    q.iterations = iterations;
+    q.image = image;
+    q.projections = projections;
+    q.out = out;
+    q.residuals = opts ? opts->residuals : nullptr;
+    q.iterations_done = opts ? opts->iterations_done : nullptr;
+    q.fp_split = opts ? opts->fp_split : 0;
+    q.bp_split = opts ? opts->bp_split : 0;
+    if (numrhos > INT32_MAX || size > INT32_MAX || nslices > INT32_MAX) return fail(ctx, SYNK_EINVAL, "size out of range");
+    return sirt_batch(ctx, 1, &q, opts ? opts->tol : 0.0, opts ? opts->grid_blocks : 0);
 }
 
 }  // namespace
@@ -412,6 +495,15 @@ int synk_SIRT3D(synk_context *ctx, float *out, const float *angles, int64_t a, c
     const float rhozero = rh[0];
     const float deltarho = rh[1] - rh[0];
     return sirt_slices(ctx, out, angles, a, rhozero, deltarho, r, size, size, nullptr, projections, iterations, nullptr);
+}
+
+int synk_sirt_resident_blocks(void) { return sirt_persistent_grid(nullptr); }
+
+int synk_sirt_batch(synk_context *ctx, int32_t nprob, const synk_sirt_problem *probs, double tol,
+                    int32_t grid_blocks) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    return sirt_batch(ctx, nprob, probs, tol, grid_blocks);
 }
 
 int synk_sirt_slices(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,

@@ -86,17 +86,24 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
     return k >= 0 ? (sum + comp) * g.lbase : 0.0f;
 }
 
-// Ray of a near-axis angle k over the whole frame, the reference's own
-// expressions (forwardprojection.fut:31-56), reading the padded frame.
-__device__ __forceinline__ float fp_exact_ray(const ProbGeom &P, int k, int r, const float *__restrict__ xpad,
-                                              const float *__restrict__ xTpad) {
+// Ray of a near-axis angle k, the reference's own expressions
+// (forwardprojection.fut:31-56), computed by the 32 lanes of a warp: lane l
+// takes rows l, l+32, ...; the lane sums are combined in a fixed order.
+// Returns the ray sum in every lane.
+__device__ __forceinline__ float fp_exact_ray_warp(const ProbGeom &P, int k, int r, const float *__restrict__ xpad,
+                                                   const float *__restrict__ xTpad) {
+    const int lane = threadIdx.x & 31;
     const AngleGeom g = load_geom(P.geom, k);
     const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));
     if (fabsf(rho) > 0.75f * (float)P.N + 2.0f) return 0.0f;
     const float intercept = __fdiv_rn(rho, g.cost);
-    float s;
-    fp_rows_exact<false>((g.flat ? xTpad : xpad) + 1, P.N + 2, P.half, g.slope, intercept, g.lbase, s);
-    return s;
+    const float *img = (g.flat ? xTpad : xpad) + 1;
+    float acc = 0.0f;
+    for (int i = -P.half + lane; i < P.half; i += 32)
+        acc = __fadd_rn(acc, fp_row_exact<false>(img, P.N + 2, P.half, g.slope, intercept, g.lbase, i));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+    return acc;
 }
 
 cudaError_t launch_angle_lists(const ProbGeom &P, int *order, int *exact, int *counts, cudaStream_t stream);

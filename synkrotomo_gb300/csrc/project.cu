@@ -175,14 +175,16 @@ __global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, 
     if (k >= 0) sino[(size_t)k * P.D + r] = v;
 }
 
-__global__ void __launch_bounds__(128) fp_exact_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
+// one warp per near-axis ray
+__global__ void __launch_bounds__(256) fp_exact_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
                                                        const float *__restrict__ xTpad, float *__restrict__ sino) {
     const int nexact = __ldg(L.counts + 2);
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= P.D) return;
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= P.D) return;                           // warp-uniform
     for (int e = blockIdx.y; e < nexact; e += gridDim.y) {
         const int k = __ldg(L.exact + e);
-        sino[(size_t)k * P.D + r] = fp_exact_ray(P, k, r, xpad, xTpad);
+        const float v = fp_exact_ray_warp(P, k, r, xpad, xTpad);
+        if ((threadIdx.x & 31) == 0) sino[(size_t)k * P.D + r] = v;
     }
 }
 
@@ -192,8 +194,8 @@ cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad,
     fp_lane_kernel<<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    dim3 ge((P.D + 127) / 128, 8);
-    fp_exact_kernel<<<ge, 128, 0, stream>>>(P, L, xpad, xTpad, sino);
+    dim3 ge((P.D + 7) / 8, 8);
+    fp_exact_kernel<<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino);
     return cudaGetLastError();
 }
 

@@ -1,17 +1,23 @@
-// Persistent SIRT kernel (futhark/SIRT.fut:27-39 for one slice,
-// futhark/SIRT3D.fut:23-28 for a stack of independent slices).
+// Persistent SIRT kernel (futhark/SIRT.fut:27-39 per slice; futhark/SIRT3D.fut:
+// 23-28 for slice stacks; any number of independent problems of uneven size).
 //
-// One cooperative launch runs every iteration of every slice:
+// One cooperative launch runs every iteration of every problem:
 //   phase FP (iteration k):  e = b - FP(x_k), rr = R*e, sum e^2 (FP64)
 //   grid barrier
 //   phase BP (iteration k):  x_{k+1} = x_k + C*BP(rr), written to the padded
 //                            image and (through shared memory) to the padded
 //                            transposed image that the next FP phase reads
 //   grid barrier
-// Work items are assigned statically (item = block + i*grid) and are all of
-// one size within a phase.  The grid barrier spins with a time limit; a block
-// that gives up records SYNK_ETIMEOUT in the status word and returns, after
-// which every other block gives up at its next barrier too.
+// Problems carry their own geometry, work split and iteration count; a
+// problem past its count (or stopped by the residual rule) drops out of both
+// phases.  Items of one problem: FP = (slice, angle group, detector block) and
+// (slice, near-axis angle, 8 detectors); BP = (slice, 32-column tile).  A
+// single problem uses a static assignment (item = block + i*grid); a batch is
+// handed out by an atomic counter, largest problems first.  The grid barrier
+// spins with a time limit; a block that gives up records SYNK_ETIMEOUT in the
+// status word and returns, after which every other block gives up at its next
+// barrier too.
+#include <limits.h>
 #include <math.h>
 
 #include "synk_internal.cuh"
@@ -73,13 +79,6 @@ __device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status, unsig
     return *s_flag != 0;
 }
 
-__device__ __forceinline__ bool slice_active(const SirtParams &p, int s, int it) {
-    if (p.tol2 <= 0.0) return true;
-    if (*(volatile const int *)(p.stop_iter + s) < it) return false;
-    const double r2 = *(volatile const double *)(p.res2 + (size_t)s * (p.iterations + 1) + it);
-    return !(r2 <= p.tol2 * p.b2[s]);
-}
-
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -92,109 +91,158 @@ struct SirtShared {
     float red4[8][4][32];
     float tile[32][33];
     double e2;
+    long long item;
     int flag;
     int any;
 };
 
-__device__ __forceinline__ void flush_e2(const SirtParams &p, int it, int slice, SirtShared &sh) {
-    if (threadIdx.x == 0 && slice >= 0) {
-        atomicAdd(p.res2 + (size_t)slice * (p.iterations + 1) + it, sh.e2);
+__device__ __forceinline__ int stop_of(const SirtProblem &q, int s) {
+    return *(volatile const int *)(q.stop_iter + s);
+}
+__device__ __forceinline__ double res2_of(const SirtProblem &q, int s, int it) {
+    return *(volatile const double *)(q.res2 + (size_t)s * (q.iterations + 1) + it);
+}
+
+// FP of iteration it is needed when the slice has not stopped before it and
+// it is at most the problem's last update (the final FP only measures).
+__device__ __forceinline__ bool fp_needed(const SirtParams &p, const SirtProblem &q, int s, int it) {
+    if (it > q.iterations || (it == q.iterations && !p.record_final)) return false;
+    return !(p.tol2 > 0.0 && stop_of(q, s) < it);
+}
+// BP (the update) of iteration it: the slice is below its count and neither
+// stopped before nor converged at x_it.
+__device__ __forceinline__ bool bp_needed(const SirtParams &p, const SirtProblem &q, int s, int it) {
+    if (it >= q.iterations) return false;
+    if (p.tol2 <= 0.0) return true;
+    if (stop_of(q, s) < it) return false;
+    return !(res2_of(q, s, it) <= p.tol2 * q.b2[s]);
+}
+
+// Next item of a phase: static (block + i*grid) or from the phase's counter.
+__device__ __forceinline__ long long next_item(const SirtParams &p, unsigned *counter, long long prev,
+                                               SirtShared &sh) {
+    if (!p.dynamic) return prev < 0 ? (long long)blockIdx.x : prev + gridDim.x;
+    __syncthreads();
+    if (threadIdx.x == 0) sh.item = (long long)atomicAdd(counter, 1u);
+    __syncthreads();
+    return sh.item;
+}
+
+// problem holding global item `item` (begin offsets ascending)
+__device__ __forceinline__ int find_problem(const SirtParams &p, long long item, bool fp) {
+    int lo = 0, hi = p.nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const long long b = fp ? p.probs[mid].fp_begin : p.probs[mid].bp_begin;
+        if (b <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// residual of one ray: e = b - fp; rr = R*e (SIRT.fut:33-36); returns e^2
+__device__ __forceinline__ double residual(const SirtProblem &q, int s, int k, int r, float fpv) {
+    const size_t pr = (size_t)q.P.a * q.P.D;
+    const size_t ray = (size_t)k * q.P.D + r;
+    const float e = __fsub_rn(q.b[(size_t)s * pr + ray], fpv);
+    q.rr[(size_t)s * pr + ray] = __fmul_rn(q.R[ray], e);
+    return (double)e * (double)e;
+}
+
+__device__ __forceinline__ void flush_e2(int it, const SirtProblem *q, int slice, SirtShared &sh) {
+    if (threadIdx.x == 0 && q) {
+        atomicAdd(q->res2 + (size_t)slice * (q->iterations + 1) + it, sh.e2);
         sh.e2 = 0.0;
     }
 }
 
-// residual of one ray: e = b - fp; rr = R*e (SIRT.fut:33-36); returns e^2
-__device__ __forceinline__ double residual(const SirtParams &p, int s, int k, int r, float fpv) {
-    const size_t pr = (size_t)p.P.a * p.P.D;
-    const size_t ray = (size_t)k * p.P.D + r;
-    const float e = __fsub_rn(p.b[(size_t)s * pr + ray], fpv);
-    p.rr[(size_t)s * pr + ray] = __fmul_rn(p.R[ray], e);
-    return (double)e * (double)e;
-}
-
 // ---- phase FP of iteration `it` ------------------------------------------------
-__device__ void fp_phase(const SirtParams &p, int it, SirtShared &sh) {
-    const ProbGeom &P = p.P;
+__device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtShared &sh) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int S = p.fp_split, G = 8 / S;                 // G detectors per item, S row parts
-    const int ngroups = __ldg(p.L.counts) + __ldg(p.L.counts + 1);
-    const int nsteep = __ldg(p.L.counts);
-    const int nexact = __ldg(p.L.counts + 2);
-    const int dblocks = (P.D + G - 1) / G;
-    const int fast_items = ngroups * dblocks;
-    const int etiles = (P.D + 255) / 256;
-    const int ips = fast_items + nexact * etiles;      // items per slice
-    const int total = ips * p.nslices;
-    const size_t np = (size_t)P.N * (P.N + 2);
-    const int part = warp % S;
-    const int jb = (int)((long long)part * P.N / S), je = (int)((long long)(part + 1) * P.N / S);
+    const long long total = p.totals[0];
+    const SirtProblem *cur = nullptr;
     int cur_slice = -1;
     if (threadIdx.x == 0) sh.e2 = 0.0;
-    for (int item = blockIdx.x; item < total; item += gridDim.x) {
-        const int s = item / ips;
-        const int rem = item - s * ips;
+    for (long long item = next_item(p, counter, -1, sh); item < total; item = next_item(p, counter, item, sh)) {
+        const int qi = find_problem(p, item, true);
+        const SirtProblem &q = p.probs[qi];
+        const ProbGeom &P = q.P;
+        const long long local = item - q.fp_begin;
+        const int s = (int)(local / q.fp_ips);
+        const int rem = (int)(local - (long long)s * q.fp_ips);
         __syncthreads();                                  // red / e2 reuse
-        if (s != cur_slice) {
-            flush_e2(p, it, cur_slice, sh);
+        if (&q != cur || s != cur_slice) {
+            flush_e2(it, cur, cur_slice, sh);
+            cur = &q;
             cur_slice = s;
         }
-        if (p.tol2 > 0.0 && *(volatile const int *)(p.stop_iter + s) < it) continue;   // slice finished earlier
+        if (!fp_needed(p, q, s, it)) continue;            // uniform over the block
+        const int S = q.fp_split, G = 8 / S;
+        const int ngroups = __ldg(q.L.counts) + __ldg(q.L.counts + 1);
+        const int nsteep = __ldg(q.L.counts);
+        const int dblocks = (P.D + G - 1) / G;
+        const int fast_items = ngroups * dblocks;
+        const size_t np = (size_t)P.N * (P.N + 2);
         double e2 = 0.0;
         if (rem < fast_items) {
+            const int part = warp % S;
+            const int jb = (int)((long long)part * P.N / S), je = (int)((long long)(part + 1) * P.N / S);
             const int grp = rem / dblocks;
             const int db = rem - grp * dblocks;
             const int r = db * G + warp / S;
-            const int k = r < P.D ? __ldg(p.L.order + grp * 32 + lane) : -1;
-            const float *img = (grp < nsteep ? p.xpad : p.xTpad) + (size_t)s * np;
+            const int k = r < P.D ? __ldg(q.L.order + grp * 32 + lane) : -1;
+            const float *img = (grp < nsteep ? q.xpad : q.xTpad) + (size_t)s * np;
             const float v = fp_lane_ray(P, k, r, img, jb, je);
             sh.red[warp][lane] = v;
             __syncthreads();
             if (part == 0 && k >= 0) {
                 float fpv = sh.red[warp][lane];
-                for (int q = 1; q < S; ++q) fpv += sh.red[warp + q][lane];
-                e2 = residual(p, s, k, r, fpv);
+                for (int t = 1; t < S; ++t) fpv += sh.red[warp + t][lane];
+                e2 = residual(q, s, k, r, fpv);
             }
         } else {
+            const int etiles = (P.D + 7) / 8;             // near-axis rays: one per warp
             const int x = rem - fast_items;
             const int e = x / etiles;
-            const int r = (x - e * etiles) * 256 + threadIdx.x;
-            if (r < P.D) {
-                const int k = __ldg(p.L.exact + e);
-                const float v = fp_exact_ray(P, k, r, p.xpad + (size_t)s * np, p.xTpad + (size_t)s * np);
-                e2 = residual(p, s, k, r, v);
+            const int r = (x - e * etiles) * 8 + warp;
+            if (r < P.D) {                                 // warp-uniform
+                const int k = __ldg(q.L.exact + e);
+                const float v = fp_exact_ray_warp(P, k, r, q.xpad + (size_t)s * np, q.xTpad + (size_t)s * np);
+                if (lane == 0) e2 = residual(q, s, k, r, v);
             }
         }
         e2 = warp_sum_d(e2);
         if (lane == 0) atomicAdd(&sh.e2, e2);
     }
     __syncthreads();
-    flush_e2(p, it, cur_slice, sh);
+    flush_e2(it, cur, cur_slice, sh);
 }
 
 // ---- phase BP of iteration `it` ------------------------------------------------
-__device__ void bp_phase(const SirtParams &p, int it, SirtShared &sh) {
-    const ProbGeom &P = p.P;
+__device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtShared &sh) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int SB = p.bp_split, RB = 8 / SB;     // angle parts, warp rows
-    const int TR = 4 * RB;                      // tile rows
-    const int tx_n = (P.N + 31) / 32, ty_n = (P.N + TR - 1) / TR;
-    const int ips = tx_n * ty_n;
-    const int total = ips * p.nslices;
-    const size_t pr = (size_t)P.a * P.D, np = (size_t)P.N * (P.N + 2);
-    const int wrow = warp / SB, part = warp % SB;
-    const int nexact = __ldg(p.L.counts + 2);
-    const bool unit = P.deltarho == 1.0f;
-    for (int item = blockIdx.x; item < total; item += gridDim.x) {
-        const int s = item / ips;
-        const int rem = item - s * ips;
+    const long long total = p.totals[1];
+    for (long long item = next_item(p, counter, -1, sh); item < total; item = next_item(p, counter, item, sh)) {
+        const int qi = find_problem(p, item, false);
+        const SirtProblem &q = p.probs[qi];
+        const ProbGeom &P = q.P;
+        const long long local = item - q.bp_begin;
+        const int s = (int)(local / q.bp_ips);
+        const int rem = (int)(local - (long long)s * q.bp_ips);
+        if (!bp_needed(p, q, s, it)) continue;            // uniform over the block
+        const int SB = q.bp_split, RB = 8 / SB;          // angle parts, warp rows
+        const int TR = 4 * RB;                           // tile rows
+        const int tx_n = (P.N + 31) / 32;
         const int ty = rem / tx_n;
         const int tx = rem - ty * tx_n;
-        if (!slice_active(p, s, it)) continue;      // uniform over the block
+        const int wrow = warp / SB, part = warp % SB;
+        const size_t pr = (size_t)P.a * P.D, np = (size_t)P.N * (P.N + 2);
         const int col = tx * 32 + lane;
         const int row0 = ty * TR + wrow;
         const float xc = (float)(col - P.half) + 0.5f;
         const float yc0 = (float)(row0 - P.half) + 0.5f;
-        const float *rr = p.rr + (size_t)s * pr;
+        const float *rr = q.rr + (size_t)s * pr;
+        const bool unit = P.deltarho == 1.0f;
         float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f}, comp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         for (int kc = 0; kc < P.a; kc += kBpChunk) {
             __syncthreads();
@@ -207,22 +255,22 @@ __device__ void bp_phase(const SirtParams &p, int it, SirtShared &sh) {
             for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], prt[m]);
         }
         float ex[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        bp_exact_angles<4>(P, p.L.exact, nexact, part, SB, rr, row0, RB, col, ex);
+        bp_exact_angles<4>(P, q.L.exact, __ldg(q.L.counts + 2), part, SB, rr, row0, RB, col, ex);
 #pragma unroll
         for (int m = 0; m < 4; ++m) sh.red4[warp][m][lane] = (sum[m] + comp[m]) + ex[m];
         __syncthreads();
-        float *xpad = p.xpad + (size_t)s * np;
+        float *xpad = q.xpad + (size_t)s * np;
         if (part == 0) {
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 float bpv = sh.red4[warp][m][lane];
-                for (int q = 1; q < SB; ++q) bpv += sh.red4[warp + q][m][lane];
+                for (int t = 1; t < SB; ++t) bpv += sh.red4[warp + t][m][lane];
                 const int row = row0 + RB * m;
                 float xi = 0.0f;
                 if (row < P.N && col < P.N) {
                     const size_t pix = (size_t)row * P.N + col;
                     float *xp = xpad + (size_t)row * (P.N + 2) + col + 1;
-                    xi = __fadd_rn(*xp, __fmul_rn(p.C[pix], bpv));             // SIRT.fut:38-39
+                    xi = __fadd_rn(*xp, __fmul_rn(q.C[pix], bpv));             // SIRT.fut:38-39
                     *xp = xi;
                 }
                 sh.tile[lane][wrow + RB * m] = xi;
@@ -230,7 +278,7 @@ __device__ void bp_phase(const SirtParams &p, int it, SirtShared &sh) {
         }
         __syncthreads();
         // transposed write: xTpad[col][row + 1] for the tile's 32 columns x TR rows
-        float *xTpad = p.xTpad + (size_t)s * np;
+        float *xTpad = q.xTpad + (size_t)s * np;
         for (int i = threadIdx.x; i < 32 * TR; i += blockDim.x) {
             const int cl = i / TR, rl = i - cl * TR;
             const int c = tx * 32 + cl, r = ty * TR + rl;
@@ -242,26 +290,58 @@ __device__ void bp_phase(const SirtParams &p, int it, SirtShared &sh) {
 __global__ void __launch_bounds__(256, 2) sirt_persistent_kernel(SirtParams p) {
     __shared__ SirtShared sh;
     const unsigned nb = gridDim.x;
-    for (int it = 0; it <= p.iterations; ++it) {
-        const bool final_fp = it == p.iterations;
-        if (final_fp && !p.record_final) break;
-        fp_phase(p, it, sh);
+    for (int it = 0; it <= p.max_iterations; ++it) {
+        // phase 2*it: FP.  Rotating counters: reset the one of the phase after next.
+        const int ph = 2 * it;
+        if (p.dynamic && blockIdx.x == 0 && threadIdx.x == 0) p.work[(ph + 1) % 3] = 0u;
+        fp_phase(p, it, p.work + ph % 3, sh);
         if (!grid_barrier(p.bar, nb, p.status, p.timeout_ns, &sh.flag)) return;
-        if (final_fp) break;
+        if (it == p.max_iterations) break;
         // stopping rule (identical decision in every block)
         if (p.tol2 > 0.0) {
             if (threadIdx.x == 0) sh.any = 0;
             __syncthreads();
-            for (int s = threadIdx.x; s < p.nslices; s += blockDim.x) {
-                if (slice_active(p, s, it)) sh.any = 1;
-                else if (blockIdx.x == 0 && p.stop_iter[s] >= p.iterations) p.stop_iter[s] = it;
+            for (int qi = 0; qi < p.nprob; ++qi) {
+                const SirtProblem &q = p.probs[qi];
+                for (int s = threadIdx.x; s < q.nslices; s += blockDim.x) {
+                    if (bp_needed(p, q, s, it)) sh.any = 1;
+                    else if (blockIdx.x == 0 && it < q.iterations && stop_of(q, s) > it) q.stop_iter[s] = it;
+                }
             }
             __syncthreads();
             if (!sh.any) break;
         }
-        bp_phase(p, it, sh);
+        const int ph2 = ph + 1;
+        if (p.dynamic && blockIdx.x == 0 && threadIdx.x == 0) p.work[(ph2 + 1) % 3] = 0u;
+        bp_phase(p, it, p.work + ph2 % 3, sh);
         if (!grid_barrier(p.bar, nb, p.status, p.timeout_ns, &sh.flag)) return;
     }
+}
+
+// Per-problem item counts and begin offsets (depend on the angle lists).
+__global__ void sirt_plan_kernel(SirtProblem *probs, int nprob, long long *totals) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long fb = 0, bb = 0;
+    for (int i = 0; i < nprob; ++i) {
+        SirtProblem &q = probs[i];
+        const int G = 8 / q.fp_split;
+        const int ngroups = q.L.counts[0] + q.L.counts[1];
+        const int nexact = q.L.counts[2];
+        q.fp_ips = ngroups * ((q.P.D + G - 1) / G) + nexact * ((q.P.D + 7) / 8);
+        const int TR = 4 * (8 / q.bp_split);
+        q.bp_ips = ((q.P.N + 31) / 32) * ((q.P.N + TR - 1) / TR);
+        q.fp_begin = fb;
+        q.bp_begin = bb;
+        fb += (long long)q.fp_ips * q.nslices;
+        bb += (long long)q.bp_ips * q.nslices;
+    }
+    totals[0] = fb;
+    totals[1] = bb;
+}
+
+cudaError_t launch_sirt_plan(SirtProblem *probs, int nprob, long long *totals, cudaStream_t stream) {
+    sirt_plan_kernel<<<1, 32, 0, stream>>>(probs, nprob, totals);
+    return cudaGetLastError();
 }
 
 // ||b_s||^2 per slice in FP64.
@@ -283,24 +363,33 @@ __global__ void sumsq_kernel(const float *__restrict__ b, size_t len, double *__
     }
 }
 
-// residuals[s][k] = sqrt(res2[s][k] / b2[s]); iterations_done[s].
-__global__ void sirt_finalize_kernel(SirtParams p, double *residuals, int *iters_done) {
-    const int s = blockIdx.x;
-    const int K = p.iterations + 1;
-    const int stop = p.stop_iter[s] < p.iterations ? p.stop_iter[s] : p.iterations;
-    if (threadIdx.x == 0 && iters_done) iters_done[s] = stop;
-    if (!residuals) return;
-    const int last = p.record_final ? p.iterations : p.iterations - 1;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        if (k > stop || k > last) continue;
-        const double b2 = p.b2[s];
-        residuals[(size_t)s * K + k] = b2 > 0.0 ? sqrt(p.res2[(size_t)s * K + k] / b2) : 0.0;
-    }
-}
-
 cudaError_t launch_sumsq(const float *b, size_t len, int nslices, double *out, cudaStream_t stream) {
     dim3 grid(64, nslices);
     sumsq_kernel<<<grid, 256, 0, stream>>>(b, len, out);
+    return cudaGetLastError();
+}
+
+// residuals[s][k] = sqrt(res2[s][k] / b2[s]); iterations_done[s].
+__global__ void sirt_finalize_kernel(SirtProblem *probs, int record_final) {
+    const SirtProblem &q = probs[blockIdx.y];
+    const int s = blockIdx.x;
+    if (s >= q.nslices) return;
+    const int K = q.iterations + 1;
+    const int stop = q.stop_iter[s] < q.iterations ? q.stop_iter[s] : q.iterations;
+    if (threadIdx.x == 0 && q.iters_done) q.iters_done[s] = stop;
+    if (!q.residuals) return;
+    const int last = record_final ? q.iterations : q.iterations - 1;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        if (k > stop || k > last) continue;
+        const double b2 = q.b2[s];
+        q.residuals[(size_t)s * K + k] = b2 > 0.0 ? sqrt(q.res2[(size_t)s * K + k] / b2) : 0.0;
+    }
+}
+
+cudaError_t launch_sirt_finalize(SirtProblem *probs, int nprob, int max_slices, int record_final,
+                                 cudaStream_t stream) {
+    dim3 grid(max_slices, nprob);
+    sirt_finalize_kernel<<<grid, 128, 0, stream>>>(probs, record_final);
     return cudaGetLastError();
 }
 
@@ -325,11 +414,6 @@ cudaError_t launch_sirt_persistent(const SirtParams &p, int grid, cudaStream_t s
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, sirt_persistent_kernel, p);
-}
-
-cudaError_t launch_sirt_finalize(const SirtParams &p, double *residuals, int *iters_done, cudaStream_t stream) {
-    sirt_finalize_kernel<<<p.nslices, 128, 0, stream>>>(p, residuals, iters_done);
-    return cudaGetLastError();
 }
 
 }  // namespace synk

@@ -1,4 +1,5 @@
-// Parameters of the persistent SIRT kernel (sirt.cu).
+// Parameters of the persistent SIRT kernel (sirt.cu): a table of independent
+// problems, each a stack of slices that share one geometry.
 #pragma once
 
 #include "synk_internal.cuh"
@@ -6,32 +7,50 @@
 
 namespace synk {
 
-struct SirtParams {
+struct SirtProblem {
     ProbGeom P;
-    const float *R;       // [a*D] row normaliser (shared by all slices)
-    const float *C;       // [N*N] column normaliser
     AngleLists L;         // angle order of the lane-per-angle projector
+    const float *R;       // [a*D] row normaliser (shared by the slices)
+    const float *C;       // [N*N] column normaliser
     const float *b;       // [nslices][a*D] sinograms
     float *xpad;          // [nslices][N][N+2] iterate, zero column on each side
     float *xTpad;         // [nslices][N][N+2] transposed iterate, same padding
     float *rr;            // [nslices][a*D] weighted residual R*(b - FP(x))
     double *res2;         // [nslices][iterations+1] sum of (b - FP(x_k))^2
     const double *b2;     // [nslices] ||b||^2
-    int *stop_iter;       // [nslices] iteration at which the stopping rule fired (init: iterations)
+    int *stop_iter;       // [nslices] iteration at which the stopping rule fired (init: INT_MAX)
+    double *residuals;    // optional out [nslices][iterations+1]: sqrt(res2/b2)
+    int *iters_done;      // optional out [nslices]
+    int nslices;
+    int iterations;
+    int fp_split;         // 1,2,4,8 warps share one ray (rows split)
+    int bp_split;         // 1,2,4,8 warps share one pixel (angles split)
+    // filled on the device by sirt_plan_kernel (they depend on the angle lists)
+    int fp_ips;           // FP work items per slice
+    int bp_ips;           // BP work items per slice
+    long long fp_begin;   // first global FP item of this problem
+    long long bp_begin;   // first global BP item of this problem
+};
+
+struct SirtParams {
+    SirtProblem *probs;   // [nprob] (device)
+    long long *totals;    // [2] FP and BP items of all problems (device, from sirt_plan_kernel)
+    int nprob;
+    int max_iterations;
     unsigned *bar;        // [2] barrier arrival count and generation
+    unsigned *work;       // [3] rotating work counters (dynamic assignment)
     int *status;          // SYNK_OK or SYNK_ETIMEOUT
     unsigned long long timeout_ns;
     double tol2;          // relative tolerance squared (0: no stopping rule)
-    int nslices;
-    int iterations;
-    int record_final;     // also measure the residual of the final iterate
-    int fp_split;         // 1,2,4,8 warps share one ray (rows split)
-    int bp_split;         // 1,2,4,8 warps share one pixel (angles split)
+    int record_final;     // also measure the residual of each problem's final iterate
+    int dynamic;          // hand out items with an atomic counter (uneven batches)
 };
 
 cudaError_t launch_sumsq(const float *b, size_t len, int nslices, double *out, cudaStream_t stream);
+cudaError_t launch_sirt_plan(SirtProblem *probs, int nprob, long long *totals, cudaStream_t stream);
 int sirt_persistent_grid(int *blocks_per_sm);
 cudaError_t launch_sirt_persistent(const SirtParams &p, int grid, cudaStream_t stream);
-cudaError_t launch_sirt_finalize(const SirtParams &p, double *residuals, int *iters_done, cudaStream_t stream);
+cudaError_t launch_sirt_finalize(SirtProblem *probs, int nprob, int max_slices, int record_final,
+                                 cudaStream_t stream);
 
 }  // namespace synk

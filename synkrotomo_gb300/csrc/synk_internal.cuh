@@ -143,39 +143,49 @@ __device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int 
     }
 }
 
-// The reference's own expressions (forwardprojection.fut:31-56), used for
-// near-axis lines: every operation rounds exactly as the f32 reference.
-// img points at pixel (0, 0) of the frame, rows `stride` floats apart.
+// One frame row of the reference's own expressions (forwardprojection.fut:
+// 32-56), used for near-axis lines: every operation rounds exactly as the f32
+// reference.  Row i is centred (i in [-half, half)); img points at pixel (0, 0)
+// of the frame, rows `stride` floats apart.  When the segment stays in one
+// pixel the reference's two quotients are not used (lines 47, 54), so they are
+// only evaluated for two-pixel rows (xdiff can be 0 for an axis-parallel ray).
+template <bool ONES>
+__device__ __forceinline__ float fp_row_exact(const float *__restrict__ img, int stride, int half, float slope,
+                                              float intercept, float lbase, int i) {
+    const float xbot = __fadd_rn(__fmul_rn((float)i, slope), intercept);
+    const float xtop = __fadd_rn(xbot, slope);
+    const int xpb = (int)floorf(xbot);
+    const int xpt = (int)floorf(xtop);
+    const bool single = xpb == xpt;
+    const bool botin = xpb >= -half && xpb < half;
+    const bool topin = (!single) && xpt >= -half && xpt < half;
+    float lxbot = lbase, lxtop = 0.0f;
+    if (!single) {
+        const float xpmax = (float)max(xpb, xpt);
+        const float xdiff = __fsub_rn(xtop, xbot);
+        lxbot = __fmul_rn(__fdiv_rn(__fsub_rn(xpmax, xbot), xdiff), lbase);
+        lxtop = __fmul_rn(__fdiv_rn(__fsub_rn(xtop, xpmax), xdiff), lbase);
+    }
+    float bot = 0.0f, top = 0.0f;
+    if constexpr (ONES) {
+        if (botin) bot = lxbot;
+        if (topin) top = lxtop;
+    } else {
+        const float *row = img + (size_t)(i + half) * stride + half;
+        if (botin) bot = __fmul_rn(lxbot, __ldg(row + xpb));
+        if (topin) top = __fmul_rn(lxtop, __ldg(row + xpt));
+    }
+    return __fadd_rn(bot, top);
+}
+
+// All rows of a near-axis line, in the reference's order.
 template <bool ONES>
 __device__ __forceinline__ void fp_rows_exact(const float *__restrict__ img, int stride, int half, float slope,
                                               float intercept, float lbase,
                                               typename FpAcc<ONES>::T &sum) {
-    const int size = stride;
     typename FpAcc<ONES>::T acc = 0;
-    for (int i = -half; i < half; ++i) {
-        const float xbot = __fadd_rn(__fmul_rn((float)i, slope), intercept);
-        const float xtop = __fadd_rn(xbot, slope);
-        const int xpb = (int)floorf(xbot);
-        const int xpt = (int)floorf(xtop);
-        const float xpmax = (float)max(xpb, xpt);
-        const float xdiff = __fsub_rn(xtop, xbot);
-        const bool single = xpb == xpt;
-        const bool botin = xpb >= -half && xpb < half;
-        const bool topin = (!single) && xpt >= -half && xpt < half;
-        const float lxbot = single ? lbase : __fmul_rn(__fdiv_rn(__fsub_rn(xpmax, xbot), xdiff), lbase);
-        const float lxtop = __fmul_rn(__fdiv_rn(__fsub_rn(xtop, xpmax), xdiff), lbase);
-        const float *row = ONES ? nullptr : img + (size_t)(i + half) * size + half;
-        float bot = 0.0f, top = 0.0f;
-        if constexpr (ONES) {
-            if (botin) bot = lxbot;
-            if (topin) top = lxtop;
-        } else {
-            if (botin) bot = __fmul_rn(lxbot, __ldg(row + xpb));
-            if (topin) top = __fmul_rn(lxtop, __ldg(row + xpt));
-        }
-        acc += ONES ? (typename FpAcc<ONES>::T)((double)bot + (double)top)
-                    : (typename FpAcc<ONES>::T)__fadd_rn(bot, top);
-    }
+    for (int i = -half; i < half; ++i)
+        acc += (typename FpAcc<ONES>::T)fp_row_exact<ONES>(img, stride, half, slope, intercept, lbase, i);
     sum = acc;
 }
 
@@ -267,7 +277,8 @@ __device__ __forceinline__ float bp_angle(const ProbGeom &P, const AngleGeom &g,
         const float hi = fmaxf(__fsub_rn(__fadd_rn(xmin, 1.0f), minx), 0.0f);
         const float diff = __fsub_rn(maxx, minx);
         const float inside = fminf(lo, hi);
-        const float prop = inside == 0.0f ? 0.0f : __fdiv_rn(inside, diff);
+        // inside/0 is +inf in the reference, capped to 1 below
+        const float prop = inside == 0.0f ? 0.0f : (diff == 0.0f ? 1.0f : __fdiv_rn(inside, diff));
         const float l = __fmul_rn(fminf(prop, 1.0f), g.lbase);
         const int det = (int)sprime;
         if (det >= 0 && det < D) acc = __fadd_rn(acc, __fmul_rn(l, ONES ? 1.0f : __ldg(sino_row + det)));

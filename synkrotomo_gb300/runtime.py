@@ -208,7 +208,7 @@ def backprojection(angles: torch.Tensor, rhozero: float, deltarho: float, size: 
 
 def sirt_slices(angles: torch.Tensor, rhozero: float, deltarho: float, numrhos: int, size: int, nslices: int,
                 image: torch.Tensor | None, projections: torch.Tensor, iterations: int, tol: float = 0.0,
-                residuals: bool = False, fp_split: int = 0, bp_split: int = 0,
+                residuals: bool = False, fp_split: int = 0, bp_split: int = 0, grid_blocks: int = 0,
                 out: torch.Tensor | None = None):
     """SIRT of ``nslices`` independent slices in one persistent launch.
 
@@ -226,12 +226,49 @@ def sirt_slices(angles: torch.Tensor, rhozero: float, deltarho: float, numrhos: 
         res = torch.full((int(nslices), int(iterations) + 1), float("nan"), dtype=torch.float64, device=dev)
     done = torch.zeros(int(nslices), dtype=torch.int32, device=dev)
     opts = _lib.SynkOptions(float(tol), res.data_ptr() if res is not None else None, done.data_ptr(),
-                            int(fp_split), int(bp_split))
+                            int(fp_split), int(bp_split), int(grid_blocks))
     rc = ctx.lib.synk_sirt_slices(ctx.handle, _ptr(out), _ptr(angles), angles.numel(), rhozero, deltarho,
                                   int(numrhos), int(size), int(nslices), _ptr(image), _ptr(projections),
                                   int(iterations), ctypes.byref(opts))
     ctx.check(rc, "sirt")
     return out, res, done
+
+
+class Problem:
+    """One problem of a batched SIRT launch (a stack of slices with one geometry)."""
+
+    def __init__(self, angles: torch.Tensor, rhozero: float, deltarho: float, numrhos: int, size: int,
+                 projections: torch.Tensor, iterations: int, nslices: int = 1, image: torch.Tensor | None = None,
+                 residuals: bool = False, fp_split: int = 0, bp_split: int = 0):
+        self.angles, self.rhozero, self.deltarho = angles, float(rhozero), float(deltarho)
+        self.numrhos, self.size, self.nslices = int(numrhos), int(size), int(nslices)
+        self.projections, self.iterations, self.image = projections, int(iterations), image
+        self.fp_split, self.bp_split = int(fp_split), int(bp_split)
+        dev = projections.device
+        self.out = torch.empty(self.nslices * self.size * self.size, dtype=torch.float32, device=dev)
+        self.residuals = (torch.full((self.nslices, self.iterations + 1), float("nan"), dtype=torch.float64,
+                                     device=dev) if residuals else None)
+        self.done = torch.zeros(self.nslices, dtype=torch.int32, device=dev)
+
+    def _desc(self):
+        return _lib.SynkProblem(self.angles.data_ptr(), self.angles.numel(), self.rhozero, self.deltarho,
+                                self.numrhos, self.size, self.nslices, self.iterations,
+                                self.image.data_ptr() if self.image is not None else None,
+                                self.projections.data_ptr(), self.out.data_ptr(),
+                                self.residuals.data_ptr() if self.residuals is not None else None,
+                                self.done.data_ptr(), self.fp_split, self.bp_split)
+
+
+def sirt_batch(problems: list, tol: float = 0.0, grid_blocks: int = 0) -> list:
+    """Every problem's SIRT in one persistent launch (``synk_sirt_batch``);
+    results land in each problem's ``out`` / ``residuals`` / ``done``."""
+    if not problems:
+        return problems
+    ctx = context(problems[0].projections.device.index)
+    arr = (_lib.SynkProblem * len(problems))(*[p._desc() for p in problems])
+    rc = ctx.lib.synk_sirt_batch(ctx.handle, len(problems), arr, float(tol), int(grid_blocks))
+    ctx.check(rc, "sirt_batch")
+    return problems
 
 
 def sirt(angles: torch.Tensor, rhozero: float, deltarho: float, image: torch.Tensor, projections: torch.Tensor,

@@ -1,0 +1,83 @@
+"""Uneven batches of independent SIRT problems in one persistent launch, and
+the autotuner of the launch shape."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cpu_ref
+from synkrotomo_gb300 import autotune, phantom
+from synkrotomo_gb300 import runtime as rt
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def _make(size, a, seed, arc=math.pi, nslices=1, noise=0.01):
+    g = phantom.geometry(size, a, arc=arc)
+    sinos = []
+    for s in range(nslices):
+        img = phantom.ellipse_phantom(size, seed + 100 * s)
+        b = cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, img)
+        sinos.append(phantom.add_noise(b, seed + s, noise))
+    return g, np.concatenate(sinos)
+
+
+def test_uneven_batch_matches_single_problem_runs(gpu):
+    # sizes, angle counts (some limited-angle), slice counts and iteration counts all differ
+    specs = [(64, 60, math.pi, 1, 20), (32, 90, 2 * math.pi / 3, 1, 35), (48, 17, math.pi, 2, 10),
+             (96, 45, math.pi, 1, 25), (16, 8, 2 * math.pi / 3, 3, 40), (80, 120, math.pi, 1, 5)]
+    problems, refs = [], []
+    for i, (size, a, arc, ns, its) in enumerate(specs):
+        g, b = _make(size, a, seed=i, arc=arc, nslices=ns)
+        problems.append(rt.Problem(_dev(g.angles), g.rhozero, g.deltarho, g.numrhos, size, _dev(b), its,
+                                   nslices=ns, residuals=True))
+        per = b.reshape(ns, -1)
+        refs.append([cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), per[s], its)
+                     for s in range(ns)])
+    rt.sirt_batch(problems)
+    for p, ref, spec in zip(problems, refs, specs):
+        x = p.out.cpu().numpy().reshape(p.nslices, -1)
+        for s in range(p.nslices):
+            assert rel_l2(x[s], ref[s]) < 1e-5, spec
+        assert np.all(p.done.cpu().numpy() == spec[4])
+        r = p.residuals.cpu().numpy()
+        assert np.all(np.isfinite(r)) and np.all(np.diff(r, axis=1) <= 1e-6)
+
+
+def test_batch_stopping_rule_per_problem(gpu):
+    specs = [(64, 60, 0), (32, 30, 1), (48, 40, 2)]
+    probs, tols = [], []
+    for size, a, seed in specs:
+        g, b = _make(size, a, seed, noise=0.0)
+        p = rt.Problem(_dev(g.angles), g.rhozero, g.deltarho, g.numrhos, size, _dev(b), 60, residuals=True)
+        probs.append(p)
+    rt.sirt_batch(probs)
+    hist = [p.residuals.cpu().numpy()[0] for p in probs]
+    tol = max(h[25] for h in hist) * 1.0001
+    probs2 = []
+    for (size, a, seed) in specs:
+        g, b = _make(size, a, seed, noise=0.0)
+        probs2.append(rt.Problem(_dev(g.angles), g.rhozero, g.deltarho, g.numrhos, size, _dev(b), 60))
+    rt.sirt_batch(probs2, tol=tol)
+    for p, h in zip(probs2, hist):
+        k = int(p.done.item())
+        assert k == next(i for i, v in enumerate(h) if v <= tol)
+
+
+def test_autotuner_picks_a_valid_shape_and_caches_it(gpu, tmp_path):
+    g, b = _make(64, 48, 0)
+    path = str(tmp_path / "tune.json")
+    ang, bd = _dev(g.angles), _dev(b)
+    c = autotune.tune_sirt(ang, g.rhozero, g.deltarho, g.numrhos, 64, bd, path=path)
+    assert c["fp_split"] in (1, 2, 4, 8) and c["bp_split"] in (1, 2, 4, 8) and c["grid_blocks"] >= 1
+    assert autotune.load_cache(path)[autotune.bucket(64, 48, g.numrhos, 1)] == c
+    x, _, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, 64, 1, None, bd, 20,
+                             fp_split=c["fp_split"], bp_split=c["bp_split"], grid_blocks=c["grid_blocks"])
+    ref = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(64 * 64, np.float32), b, 20)
+    assert rel_l2(x.cpu().numpy(), ref) < 1e-5
