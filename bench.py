@@ -33,23 +33,35 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-N_SIZE, N_ANGLES, N_DET = 2048, 2048, 2897
+N_SIZE, N_ANGLES, N_DET = 2048, 2048, 2897     # the projector microbench's dense configuration
 METRIC = "SIRT ms to rel. residual 1e-3: warm-start vs plain, 1 GB300; FP/BP GB/s"
-WORKLOAD = "projector microbench, dense on-the-fly: N=2048 image, 2048 angles in [0,pi), 2897 detectors, deltarho=1"
+LEGS = ("proj", "e2e", "sirt", "csr", "cpu")      # default legs; "batch" and "stack" on request
 
 
-def step_bytes(N=N_SIZE, a=N_ANGLES, D=N_DET):
-    return 8 * (N * N + a * D)
+def set_workload(size, angles, detectors):
+    """Smaller cases of the same workload (profiling); the defaults are the benchmark."""
+    global N_SIZE, N_ANGLES, N_DET
+    N_SIZE, N_ANGLES = int(size), int(angles)
+    N_DET = int(detectors) if detectors else int(math.ceil(N_SIZE * math.sqrt(2.0)))
 
 
-def flops_fp(N=N_SIZE, a=N_ANGLES, D=N_DET):
+def workload_name():
+    return (f"projector microbench, dense on-the-fly: N={N_SIZE} image, {N_ANGLES} angles in [0,pi), "
+            f"{N_DET} detectors, deltarho=1")
+
+
+def step_bytes():
+    return 8 * (N_SIZE * N_SIZE + N_ANGLES * N_DET)
+
+
+def flops_fp():
     # 14 flops per ray-row step (forwardprojection.fut:32-56; FMA=2, add/mul/div=1)
-    return 14.0 * a * D * N
+    return 14.0 * N_ANGLES * N_DET * N_SIZE
 
 
-def flops_bp(N=N_SIZE, a=N_ANGLES, rpp=2):
+def flops_bp(rpp=2):
     # 13 flops per (pixel, line) + 13 per ray evaluation (backprojection.fut:49-64)
-    return (13.0 + 13.0 * rpp) * N * N * a
+    return (13.0 + 13.0 * rpp) * N_SIZE * N_SIZE * N_ANGLES
 
 
 def workload(seed=0):
@@ -254,11 +266,14 @@ def run_gpu(args, rank, world):
         torch.distributed.barrier()
 
     # end to end through the public API, pinned host buffers
-    e2e = run_e2e(args, g, img, sino, dev)
-    sirt = run_sirt_cfg0(dev) if (rank == 0 and not args.skip_sirt) else None
-    csr = run_csr_cfg1(dev) if (rank == 0 and not args.skip_csr) else None
+    e2e = run_e2e(args, g, img, sino, dev) if "e2e" in args.legs else None
+    sirt = run_sirt_cfg0(dev) if (rank == 0 and "sirt" in args.legs) else None
+    csr = run_csr_cfg1(dev) if (rank == 0 and "csr" in args.legs) else None
+    batch = run_batch_cfg3(dev) if (rank == 0 and "batch" in args.legs) else None
+    stack = run_stack_cfg2(dev) if (rank == 0 and "stack" in args.legs) else None
     return {"step_ms": step_ms, "fp_ms": statistics.median(fp_ms), "bp_ms": statistics.median(bp_ms),
-            "wall_s": wall, "clocks": clk.summary(), "e2e": e2e, "sirt": sirt, "csr": csr,
+            "wall_s": wall, "clocks": clk.summary(), "e2e": e2e, "sirt": sirt, "csr": csr, "batch": batch,
+            "stack": stack,
             "sms": torch.cuda.get_device_properties(dev).multi_processor_count}
 
 
@@ -369,16 +384,100 @@ def run_csr_cfg1(dev, reps=20):
     return out
 
 
+def run_batch_cfg3(dev, seed=0, n_problems=64, iterations=150):
+    """The uneven batch: 64 independent problems, N from {128,...,1024}, angle
+    counts from {60,...,1024}, a quarter limited-angle ([0, 2pi/3)),
+    ceil(N*sqrt(2)) detectors, 0.5-2 % noise, 150 iterations, in one launch;
+    compared with the same problems run one launch each."""
+    import torch
+
+    from synkrotomo_gb300 import phantom
+    from synkrotomo_gb300 import runtime as rt
+
+    rng = np.random.default_rng(seed)
+    probs_spec = []
+    for i in range(n_problems):
+        N = int(rng.choice([128, 256, 384, 512, 768, 1024]))
+        a = int(rng.choice([60, 90, 180, 360, 720, 1024]))
+        limited = rng.random() < 0.25
+        noise = float(rng.uniform(0.005, 0.02))
+        probs_spec.append((N, a, limited, noise))
+    problems = []
+    work = 0.0
+    for i, (N, a, limited, noise) in enumerate(probs_spec):
+        g = phantom.geometry(N, a, arc=(2 * math.pi / 3) if limited else math.pi)
+        ang = torch.from_numpy(g.angles).to(dev)
+        img = torch.from_numpy(phantom.ellipse_phantom(N, seed + i)).to(dev)
+        b = rt.forwardprojection(ang, g.rhozero, g.deltarho, g.numrhos, img)
+        b = b + torch.randn_like(b) * (noise * float(b.max()))
+        problems.append(rt.Problem(ang, g.rhozero, g.deltarho, g.numrhos, N, b, iterations))
+        work += (N * N * a + a * g.numrhos * N) * iterations
+    torch.cuda.synchronize()
+    rt.sirt_batch(problems)            # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    rt.sirt_batch(problems)
+    e1.record()
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1)
+    e0.record()
+    for p in problems:
+        rt.sirt_batch([p])
+    e1.record()
+    torch.cuda.synchronize()
+    seq_ms = e0.elapsed_time(e1)
+    return {"problems": n_problems, "iterations": iterations, "ms_one_launch": batch_ms,
+            "ms_one_launch_per_problem": seq_ms, "pixel_angle_and_ray_row_steps": work,
+            "sizes": sorted({s[0] for s in probs_spec}), "angle_counts": sorted({s[1] for s in probs_spec})}
+
+
+def run_stack_cfg2(dev, nslices=64, iterations=100, seed=0):
+    """The slice stack (512 x 512 slices, 360 angles in [0,pi), 725 detectors,
+    1 % noise, 100 iterations) for `nslices` of the 512 slices in one
+    persistent launch; ms for the full 512-slice stack scaled linearly."""
+    import torch
+
+    from synkrotomo_gb300 import phantom
+    from synkrotomo_gb300 import runtime as rt
+
+    N = 512
+    g = phantom.geometry(N, 360, numrhos=725)
+    ang = torch.from_numpy(g.angles).to(dev)
+    vol = phantom.ellipsoid_volume(N, 512, seed)[256 - nslices // 2: 256 + nslices // 2]
+    sinos = []
+    for z in range(nslices):
+        b = rt.forwardprojection(ang, g.rhozero, g.deltarho, g.numrhos, torch.from_numpy(vol[z]).to(dev))
+        sinos.append(b + torch.randn_like(b) * (0.01 * float(b.max())))
+    b = torch.cat(sinos)
+    prob = rt.Problem(ang, g.rhozero, g.deltarho, g.numrhos, N, b, iterations, nslices=nslices)
+    rt.sirt_batch([prob])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    rt.sirt_batch([prob])
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"slices_run": nslices, "iterations": iterations, "ms": ms, "ms_512_slices_scaled": ms * 512 / nslices,
+            "ms_per_slice_iteration": ms / (nslices * iterations)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--skip-sirt", action="store_true")
-    ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--skip-csr", action="store_true")
+    ap.add_argument("--legs", default=",".join(LEGS),
+                    help="comma list of: proj (device-resident FP+BP, always run), e2e, sirt, csr, cpu, "
+                         "batch (64 uneven problems), stack (slice stack)")
+    ap.add_argument("--size", type=int, default=2048, help="image side (profiling cases; default: the benchmark)")
+    ap.add_argument("--angles", type=int, default=2048)
+    ap.add_argument("--detectors", type=int, default=0, help="0: ceil(size*sqrt(2))")
     args = ap.parse_args()
+    args.legs = set(x.strip() for x in args.legs.split(",") if x.strip()) | {"proj"}
+    set_workload(args.size, args.angles, args.detectors)
     args.warmup = max(3, args.warmup)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -398,7 +497,7 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "l2": "n/a (host CPU)"},
+                "config": {"workload": workload_name(), "l2": "n/a (host CPU)"},
                 "cpu_baseline": {"value": value, "unit": "GB/s", "cores": r["cores"], "kind": "port",
                                  "sample": f"{r['sample_angles']} of {N_ANGLES} angles per step, scaled x"
                                            f"{N_ANGLES / r['sample_angles']:.1f} (oracle/cpu_ref.c, "
@@ -430,25 +529,26 @@ def main():
     bp_tf = flops_bp() / (res["bp_ms"] * 1e-3) / 1e12
     dom = "bp" if res["bp_ms"] >= res["fp_ms"] else "fp"
     achieved = bp_tf if dom == "bp" else fp_tf
-    kname = "bp_kernel_dense2048" if dom == "bp" else "fp_kernel_dense2048"
-    roofline = {"bound": "fp32", "kernel": "bp_kernel" if dom == "bp" else "fp_kernel", "achieved": achieved,
+    kname = "bp_tile_kernel" if dom == "bp" else "fp_lane_kernel"
+    roofline = {"bound": "fp32", "kernel": kname, "achieved": achieved,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                "traffic": ncu_traffic(kname),
+                "traffic": ncu_traffic(f"{kname}_dense{N_SIZE}") if N_SIZE == 2048 else None,
                 "peak_source": f"nominal FP32: {res['sms']} SMs x 128 FMA/clk x 2 x {sm_max:.0f} MHz "
                                "(MEASURED_PEAKS.json has no FP32 figure)",
                 "fp_tflops": fp_tf, "bp_tflops": bp_tf}
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res["step_ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "image": N_SIZE, "angles": N_ANGLES, "detectors": N_DET,
+            "config": {"workload": workload_name(), "image": N_SIZE, "angles": N_ANGLES, "detectors": N_DET,
                        "step": "forward projection + backprojection", "l2": "flushed (512 MB write) before every step",
                        "parallelism": f"replicas x{world}"},
             "fp_ms": res["fp_ms"], "bp_ms": res["bp_ms"],
             "gpu_launches": 8 * args.steps,
             "clocks": res["clocks"], "roofline": roofline}
     e = res["e2e"]
-    line["e2e"] = {"value": world * step_bytes() / (e["ms"] * 1e-3) / 1e9, "unit": "GB/s",
-                   "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["ms"]}
+    if e is not None:
+        line["e2e"] = {"value": world * step_bytes() / (e["ms"] * 1e-3) / 1e9, "unit": "GB/s",
+                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["ms"]}
     if res["sirt"] is not None:
         line["sirt_cfg0"] = res["sirt"]
     if res["csr"] is not None:
@@ -458,7 +558,10 @@ def main():
             c[k]["frac_hbm"] = c[k]["GB/s"] / hbm
         c["hbm_peak_gbs"] = hbm
         line["csr_cfg1"] = c
-    if not args.skip_cpu:
+    for key in ("batch", "stack"):
+        if res[key] is not None:
+            line[{"batch": "sirt_batch_cfg3", "stack": "sirt_stack_cfg2"}[key]] = res[key]
+    if "cpu" in args.legs:
         r = cpu_reference_rate(budget_s=10.0)
         cv = step_bytes() / r["step_s"] / 1e9
         line["cpu_baseline"] = {"value": cv, "unit": "GB/s", "cores": r["cores"], "kind": "port",
