@@ -199,6 +199,50 @@ int synk_spmv_csr32(synk_context *ctx, int64_t rows, const int32_t *rowptr, cons
 int synk_backprojection_noalloc(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
                                 float deltarho, int32_t size, const float *projections, int64_t p);
 
+/* ---- BF16 tensor-core building blocks of the U-Net warm starter (no reference
+ * counterpart).  BF16 arrays are passed as uint16_t bit patterns, NHWC. ---- */
+
+/* C[M x N] (FP32) = A[M x K] * B[N x K]^T, A and B BF16 row-major (K
+ * contiguous).  M % 128 == 0, 16 <= N <= 256, N % 16 == 0, K % 64 == 0. */
+int synk_gemm_bf16(synk_context *ctx, const uint16_t *A, const uint16_t *B, float *C, int32_t M, int32_t N,
+                   int32_t K);
+
+/* 3x3 convolution, padding 1: y[b,h,w,yoff+o] = epi(sum_{tap,i} x[b,h+ky-1,w+kx-1,xoff+i]
+ * * w[o][(ky*3+kx)*Cin + i]) with x [B][H][W][ldx], y [B][H][W][ldy], w [Cout][9*Cin].
+ * epi: 1 = relu(. + bias), 4 = . + bias, 2 = . * (mask[b,h,w,moff+o] > 0).
+ * Cin % 32 == 0, Cout % 16 == 0, Cout <= 256, H*W a multiple of 128 tiles. */
+int synk_conv3x3_bf16(synk_context *ctx, const uint16_t *x, int32_t ldx, int32_t xoff, int32_t Cin, int32_t B,
+                      int32_t H, int32_t W, const uint16_t *w, const float *bias, uint16_t *y, int32_t ldy,
+                      int32_t yoff, int32_t Cout, int32_t epi, const uint16_t *mask, int32_t ldm, int32_t moff);
+
+/* dw[o][tap*Cin + i] += sum_p dy[p][o] * x[p + tap][i] from channel-major
+ * dyT [Cout][B][H][W] and the three W-shifted channel-major copies
+ * xT3 [3][Cin][B][H][W]; dw FP32 [Cout][9*Cin]. */
+int synk_conv3x3_wgrad_bf16(synk_context *ctx, const uint16_t *dyT, const uint16_t *xT3, float *dw, int32_t Cin,
+                            int32_t Cout, int32_t B, int32_t H, int32_t W, int32_t ksplit);
+
+/* ---- U-Net warm starter (no reference counterpart) ----
+ * 4 levels, 32 base channels, 3x3 convolutions + ReLU, BF16 activations, FP32
+ * accumulation and FP32 master weights; input the normalised backprojection
+ * C*A^T*R*b, output a start image for SIRT (x + a learned correction).
+ * Images are FP32 [batch][size][size] device arrays; size is a multiple of 256. */
+typedef struct synk_unet synk_unet;
+
+int synk_unet_new(synk_context *ctx, synk_unet **out, int32_t max_batch, int32_t size, uint64_t seed);
+void synk_unet_free(synk_unet *net);
+int64_t synk_unet_num_params(const synk_unet *net);
+/* direction 0: copy the FP32 parameters to dst; 1: load them from dst. */
+int synk_unet_params(synk_context *ctx, synk_unet *net, float *dst, int32_t direction);
+/* y = net(x) for `batch` images. */
+int synk_unet_forward(synk_context *ctx, synk_unet *net, const float *x, float *y, int32_t batch);
+/* One training step on (x, target) with the MSE loss: forward, backward and,
+ * when apply != 0, one fused Adam update with learning rate lr (beta 0.9 /
+ * 0.999, eps 1e-8).  loss (optional device double) receives the batch loss. */
+int synk_unet_train_step(synk_context *ctx, synk_unet *net, const float *x, const float *target, int32_t batch,
+                         float lr, int32_t apply, double *loss);
+/* FP32 gradients of the last train step run with apply = 0 (same layout as the parameters). */
+int synk_unet_gradients(synk_context *ctx, synk_unet *net, float *dst);
+
 #ifdef __cplusplus
 }
 #endif

@@ -100,6 +100,25 @@ SIGNATURES = {
     "synk_csr_spmv_t": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "synk_spmv_csr32": (ctypes.c_int, [c_ctx, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p]),
+    "synk_gemm_bf16": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_int32]),
+    "synk_conv3x3_bf16": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                         ctypes.c_int32]),
+    "synk_conv3x3_wgrad_bf16": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                               ctypes.c_int32, ctypes.c_int32]),
+    "synk_unet_new": (ctypes.c_int, [c_ctx, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_uint64]),
+    "synk_unet_free": (None, [ctypes.c_void_p]),
+    "synk_unet_num_params": (ctypes.c_int64, [ctypes.c_void_p]),
+    "synk_unet_params": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "synk_unet_forward": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "synk_unet_train_step": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                            ctypes.c_float, ctypes.c_int32, ctypes.c_void_p]),
+    "synk_unet_gradients": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p]),
     "synk_backprojection_noalloc": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                                    ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_void_p,
                                                    ctypes.c_int64]),

@@ -15,6 +15,8 @@
 #include "sirt_internal.cuh"
 #include "csr_internal.cuh"
 #include "fp_tile.cuh"
+#include "umma_gemm.cuh"
+#include "unet.cuh"
 
 using namespace synk;
 
@@ -521,6 +523,130 @@ static void csr_release(synk_csr *m) {
     cudaFree(m->idx); cudaFree(m->idx_t);
     cudaFree(m->vals); cudaFree(m->vals_t);
     delete m;
+}
+
+int synk_gemm_bf16(synk_context *ctx, const uint16_t *A, const uint16_t *B, float *C, int32_t M, int32_t N,
+                   int32_t K) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!A || !B || !C) return fail(ctx, SYNK_EINVAL, "null pointer");
+    if (M <= 0 || M % 128 || N < 16 || N > 256 || N % 16 || K <= 0 || K % 64)
+        return fail(ctx, SYNK_EINVAL, "gemm shape M=%d N=%d K=%d not supported", M, N, K);
+    SYNK_CUDA(unet::gemm_bf16(A, B, C, M, N, K, ctx->d_status, ctx->barrier_timeout_ns, ctx->stream), "tcgen05 gemm");
+    return SYNK_OK;
+}
+
+int synk_conv3x3_bf16(synk_context *ctx, const uint16_t *x, int32_t ldx, int32_t xoff, int32_t Cin, int32_t B,
+                      int32_t H, int32_t W, const uint16_t *w, const float *bias, uint16_t *y, int32_t ldy,
+                      int32_t yoff, int32_t Cout, int32_t epi, const uint16_t *mask, int32_t ldm, int32_t moff) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!x || !w || !y) return fail(ctx, SYNK_EINVAL, "null pointer");
+    if ((epi == unet::EPI_BIAS_RELU || epi == unet::EPI_BIAS) && !bias) return fail(ctx, SYNK_EINVAL, "null bias");
+    if (epi == unet::EPI_MASK && !mask) return fail(ctx, SYNK_EINVAL, "null mask");
+    if (B <= 0 || H <= 0 || W <= 0) return fail(ctx, SYNK_EINVAL, "bad image shape");
+    unet::ConvArgs c = {x, ldx, xoff, Cin, B, H, W, w, bias, y, ldy, yoff, Cout, mask, ldm, moff};
+    cudaError_t e = unet::conv3x3(c, epi, ctx->d_status, ctx->barrier_timeout_ns, ctx->stream);
+    if (e == cudaErrorInvalidValue) return fail(ctx, SYNK_EINVAL, "conv3x3 shape not supported (Cin=%d Cout=%d H=%d W=%d)", Cin, Cout, H, W);
+    SYNK_CUDA(e, "tcgen05 conv3x3");
+    return SYNK_OK;
+}
+
+int synk_conv3x3_wgrad_bf16(synk_context *ctx, const uint16_t *dyT, const uint16_t *xT3, float *dw, int32_t Cin,
+                            int32_t Cout, int32_t B, int32_t H, int32_t W, int32_t ksplit) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!dyT || !xT3 || !dw) return fail(ctx, SYNK_EINVAL, "null pointer");
+    if (B <= 0 || H <= 0 || W <= 0 || ksplit < 1) return fail(ctx, SYNK_EINVAL, "bad shape");
+    unet::WgradArgs a = {dyT, xT3, dw, Cin, Cout, B, H, W, ksplit};
+    cudaError_t e = unet::conv3x3_wgrad(a, ctx->d_status, ctx->barrier_timeout_ns, ctx->stream);
+    if (e == cudaErrorInvalidValue) return fail(ctx, SYNK_EINVAL, "wgrad shape not supported");
+    SYNK_CUDA(e, "tcgen05 wgrad");
+    return SYNK_OK;
+}
+
+struct synk_unet {
+    int device = 0;
+    int size = 0, max_batch = 0;
+    unet::Net *net = nullptr;
+};
+
+int synk_unet_new(synk_context *ctx, synk_unet **out, int32_t max_batch, int32_t size, uint64_t seed) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out) return fail(ctx, SYNK_EINVAL, "null pointer");
+    *out = nullptr;
+    if (size < 256 || size % 256 || size > 4096) return fail(ctx, SYNK_EINVAL, "U-Net size must be a multiple of 256 (got %d)", size);
+    if (max_batch < 1 || max_batch > 1024) return fail(ctx, SYNK_EINVAL, "bad batch %d", max_batch);
+    unet::Net *n = nullptr;
+    SYNK_CUDA(unet::net_create(&n, max_batch, size, seed, ctx->stream), "U-Net allocation");
+    synk_unet *h = new synk_unet();
+    h->device = ctx->device;
+    h->size = size;
+    h->max_batch = max_batch;
+    h->net = n;
+    *out = h;
+    return SYNK_OK;
+}
+
+void synk_unet_free(synk_unet *net) {
+    if (!net) return;
+    cudaSetDevice(net->device);
+    cudaDeviceSynchronize();
+    unet::net_free(net->net);
+    delete net;
+}
+
+int64_t synk_unet_num_params(const synk_unet *net) { return net ? unet::net_nparams(net->net) : 0; }
+
+int synk_unet_params(synk_context *ctx, synk_unet *net, float *dst, int32_t direction) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!net || !dst) return fail(ctx, SYNK_EINVAL, "null pointer");
+    const size_t bytes = sizeof(float) * (size_t)unet::net_nparams(net->net);
+    if (direction == 0) {
+        SYNK_CUDA(cudaMemcpyAsync(dst, unet::net_params(net->net), bytes, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+    } else {
+        SYNK_CUDA(cudaMemcpyAsync(unet::net_params(net->net), dst, bytes, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        SYNK_CUDA(unet::net_refresh_weights(net->net, ctx->stream), "weight copies");
+    }
+    return SYNK_OK;
+}
+
+int synk_unet_forward(synk_context *ctx, synk_unet *net, const float *x, float *y, int32_t batch) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!net || !x || !y) return fail(ctx, SYNK_EINVAL, "null pointer");
+    if (batch < 1 || batch > net->max_batch) return fail(ctx, SYNK_EINVAL, "batch %d outside [1, %d]", batch, net->max_batch);
+    SYNK_CUDA(unet::net_forward(net->net, batch, x, y, nullptr, ctx->d_status, ctx->barrier_timeout_ns, ctx->stream),
+              "U-Net forward");
+    return SYNK_OK;
+}
+
+int synk_unet_train_step(synk_context *ctx, synk_unet *net, const float *x, const float *target, int32_t batch,
+                         float lr, int32_t apply, double *loss) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!net || !x || !target) return fail(ctx, SYNK_EINVAL, "null pointer");
+    if (batch < 1 || batch > net->max_batch) return fail(ctx, SYNK_EINVAL, "batch %d outside [1, %d]", batch, net->max_batch);
+    if (!(lr >= 0.0f) || !isfinite(lr)) return fail(ctx, SYNK_EINVAL, "bad learning rate");
+    unet::Net *n = net->net;
+    cudaStream_t st = ctx->stream;
+    SYNK_CUDA(cudaMemsetAsync(unet::net_grads(n), 0, sizeof(float) * (size_t)unet::net_nparams(n), st), "zero grads");
+    SYNK_CUDA(unet::net_forward(n, batch, x, nullptr, target, ctx->d_status, ctx->barrier_timeout_ns, st), "U-Net forward");
+    SYNK_CUDA(unet::net_backward(n, batch, ctx->d_status, ctx->barrier_timeout_ns, st), "U-Net backward");
+    if (loss) SYNK_CUDA(cudaMemcpyAsync(loss, unet::net_loss(n), sizeof(double), cudaMemcpyDeviceToDevice, st), "loss");
+    if (apply) SYNK_CUDA(unet::net_adam(n, lr, st), "Adam");
+    return SYNK_OK;
+}
+
+int synk_unet_gradients(synk_context *ctx, synk_unet *net, float *dst) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!net || !dst) return fail(ctx, SYNK_EINVAL, "null pointer");
+    const size_t bytes = sizeof(float) * (size_t)unet::net_nparams(net->net);
+    SYNK_CUDA(cudaMemcpyAsync(dst, unet::net_grads(net->net), bytes, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+    return SYNK_OK;
 }
 
 int synk_csr_new(synk_context *ctx, synk_csr **out, const float *angles, int64_t a, float rhozero, float deltarho,
