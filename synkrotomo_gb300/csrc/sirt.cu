@@ -287,7 +287,7 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
     }
 }
 
-__global__ void __launch_bounds__(256, 2) sirt_persistent_kernel(SirtParams p) {
+__global__ void __launch_bounds__(256, 3) sirt_persistent_kernel(SirtParams p) {
     __shared__ SirtShared sh;
     const unsigned nb = gridDim.x;
     for (int it = 0; it <= p.max_iterations; ++it) {

@@ -1,0 +1,242 @@
+"""Learned warm start for SIRT: data, training and evaluation.
+
+Pipeline (everything on the GPU, through libsynk):
+  data      seeded random-ellipse phantoms -> forward projection -> Gaussian
+            noise (sigma = 1 % of the sinogram maximum); input = one SIRT
+            update from zero, i.e. the normalised backprojection C*A^T*R*b;
+            target = SIRT after `target_iters` updates (1000)
+  training  the U-Net (synkrotomo_gb300.unet) with MSE loss and Adam
+  use       x0 = net(C*A^T*R*b); SIRT from x0 until the relative data
+            residual ||Ax - b|| / ||b|| reaches r*, the residual plain
+            zero-start SIRT reaches after `budget` iterations; when the warm
+            start's own residual exceeds the zero start's (1.0), the zero
+            start is used instead
+The comparison (iterations and milliseconds to r*) is against plain
+zero-start SIRT on the same sinograms.
+
+Run ``python -m synkrotomo_gb300.warmstart --help`` for the full experiment.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import phantom
+from . import runtime as rt
+from .unet import UNet
+
+
+def ellipse_batch(n: int, size: int, seed: int, n_ellipses: int = 10, device="cuda") -> torch.Tensor:
+    """n random-ellipse phantoms [n, size*size] (float32, on the device):
+    centres U[-0.6, 0.6]*N/2, semi-axes U[0.05, 0.4]*N/2, rotation U[0, pi),
+    additive intensity U[0, 1]; seeded per batch."""
+    g = torch.Generator(device="cpu").manual_seed(int(seed))
+    p = torch.rand(n, n_ellipses, 6, generator=g, dtype=torch.float64).to(device)
+    half = size / 2.0
+    cx = (p[..., 0] * 1.2 - 0.6) * half
+    cy = (p[..., 1] * 1.2 - 0.6) * half
+    ax = (0.05 + 0.35 * p[..., 2]) * half
+    ay = (0.05 + 0.35 * p[..., 3]) * half
+    phi = p[..., 4] * math.pi
+    val = p[..., 5]
+    coords = torch.arange(size, device=device, dtype=torch.float64) - half + 0.5
+    yy, xx = torch.meshgrid(coords, coords, indexing="ij")
+    img = torch.zeros(n, size, size, device=device, dtype=torch.float64)
+    for e in range(n_ellipses):
+        c, s = torch.cos(phi[:, e])[:, None, None], torch.sin(phi[:, e])[:, None, None]
+        dx, dy = xx[None] - cx[:, e, None, None], yy[None] - cy[:, e, None, None]
+        u, v = dx * c + dy * s, -dx * s + dy * c
+        inside = (u / ax[:, e, None, None]) ** 2 + (v / ay[:, e, None, None]) ** 2 <= 1.0
+        img += inside * val[:, e, None, None]
+    return img.float().reshape(n, size * size)
+
+
+class Problem:
+    """Geometry of one warm-start configuration."""
+
+    def __init__(self, size: int, n_angles: int, noise: float = 0.01):
+        self.size, self.n_angles, self.noise = int(size), int(n_angles), float(noise)
+        self.g = phantom.geometry(self.size, self.n_angles)
+        self.angles = torch.from_numpy(self.g.angles).cuda()
+
+    def sinograms(self, imgs: torch.Tensor, seed: int) -> torch.Tensor:
+        """[n, a*D] noisy sinograms of [n, N*N] images."""
+        g = self.g
+        out = torch.empty(imgs.shape[0], g.n_rays, device=imgs.device)
+        for i in range(imgs.shape[0]):
+            rt.forwardprojection(self.angles, g.rhozero, g.deltarho, g.numrhos, imgs[i], out=out[i])
+        gen = torch.Generator(device=imgs.device).manual_seed(int(seed) + 99991)
+        sigma = self.noise * out.amax(dim=1, keepdim=True)
+        return out + sigma * torch.randn(out.shape, device=imgs.device, generator=gen)
+
+    def sirt(self, sinos: torch.Tensor, iterations: int, start: torch.Tensor | None = None, tol: float = 0.0,
+             residuals: bool = False):
+        g = self.g
+        n = sinos.shape[0]
+        x, res, done = rt.sirt_slices(self.angles, g.rhozero, g.deltarho, g.numrhos, self.size, n,
+                                      None if start is None else start.reshape(-1).contiguous(),
+                                      sinos.reshape(-1).contiguous(), iterations, tol=tol, residuals=residuals)
+        return x.view(n, -1), res, done
+
+
+def make_dataset(prob: Problem, n: int, seed: int, target_iters: int = 1000, chunk: int = 256):
+    """inputs (normalised backprojections) and targets (SIRT after target_iters)."""
+    xs, ts = [], []
+    for c0 in range(0, n, chunk):
+        k = min(chunk, n - c0)
+        imgs = ellipse_batch(k, prob.size, seed * 1000003 + c0)
+        b = prob.sinograms(imgs, seed * 1000003 + c0)
+        x1, _, _ = prob.sirt(b, 1)
+        xt, _, _ = prob.sirt(b, target_iters)
+        xs.append(x1)
+        ts.append(xt)
+    return torch.cat(xs), torch.cat(ts)
+
+
+def train(net: UNet, inputs: torch.Tensor, targets: torch.Tensor, epochs: int, batch: int = 32, lr: float = 1e-3,
+          seed: int = 0, log=None):
+    n = inputs.shape[0]
+    N = net.size
+    hist = []
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=g)
+        losses = []
+        for i in range(0, n - batch + 1, batch):
+            idx = perm[i:i + batch].cuda()
+            loss = net.train_step(inputs[idx].view(batch, N, N), targets[idx].view(batch, N, N), lr=lr)
+            losses.append(loss.clone())
+        ep_loss = float(torch.stack(losses).mean().item())
+        hist.append(ep_loss)
+        if log:
+            log(f"epoch {ep}: loss {ep_loss:.6g}")
+    return hist
+
+
+def first_below(hist: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
+    """Per row, the first iteration k with hist[k] <= target (hist.shape[1] if none)."""
+    ok = hist <= target[:, None]
+    k = torch.where(ok.any(dim=1), ok.float().argmax(dim=1), torch.full_like(target, hist.shape[1]).long())
+    return k
+
+
+def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 100, 200), max_iters: int = 600):
+    """Plain zero-start SIRT vs warm-started SIRT on n held-out images.
+
+    For each plain budget K: r*_i = 1.01 x the residual plain SIRT reaches on
+    image i after K iterations; iterations to r*_i come from full residual
+    histories (plain and warm, one run each).  Milliseconds are measured on
+    batched runs that stop at the loosest r* of the batch (one stopping level
+    per launch), the warm run including the normalised backprojection and
+    the network."""
+    K = max(budgets)
+    imgs = ellipse_batch(n, prob.size, seed)
+    b = prob.sinograms(imgs, seed)
+    _, hp, _ = prob.sirt(b, K, residuals=True)
+    x1, _, _ = prob.sirt(b, 1)
+    x0 = net.forward(x1.view(n, prob.size, prob.size)).view(n, -1)
+    _, hw, _ = prob.sirt(b, max_iters, start=x0, residuals=True)
+    fallback = hw[:, 0] > 1.0          # the warm start is worse than the zero start
+    rows = []
+    for Kb in budgets:
+        rstar = hp[:, Kb] * 1.01
+        it_plain = first_below(hp, rstar).float()
+        it_warm = torch.where(fallback, it_plain, first_below(hw, rstar).float())
+        tol = float(rstar.max().item())
+        ms = {}
+        for label in ("plain", "warm"):
+            for rep in range(2):                       # first run warms up
+                torch.cuda.synchronize()
+                t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                t0.record()
+                start = None
+                if label == "warm":
+                    xa, _, _ = prob.sirt(b, 1)
+                    start = net.forward(xa.view(n, prob.size, prob.size)).view(n, -1)
+                _, _, done = prob.sirt(b, max_iters, start=start, tol=tol)
+                t1.record()
+                torch.cuda.synchronize()
+            ms[label] = t0.elapsed_time(t1)
+        rows.append({"budget": Kb, "target_residual_mean": float(rstar.mean().item()),
+                     "plain_iterations_mean": float(it_plain.mean().item()),
+                     "warm_iterations_mean": float(it_warm.mean().item()),
+                     "speedup_iterations": float(it_plain.mean().item() / max(it_warm.mean().item(), 1e-9)),
+                     "batched_ms_plain": ms["plain"], "batched_ms_warm": ms["warm"],
+                     "speedup_ms": ms["plain"] / max(ms["warm"], 1e-9)})
+    return {"n": n, "size": prob.size, "angles": prob.n_angles,
+            "warm_start_residual_mean": float(hw[:, 0].mean().item()),
+            "plain_residual_after_1": float(hp[:, 1].mean().item()),
+            "fallback_images": int(fallback.sum().item()), "budgets": rows}
+
+
+def oracle_check(net: UNet, prob: Problem, seed: int, iterations: int = 30) -> dict:
+    """Warm-started GPU SIRT against the FP64 oracle's SIRT from the same
+    start (one held-out image; test-infrastructure oracle, CPU)."""
+    from oracle import fut_ref
+    imgs = ellipse_batch(1, prob.size, seed)
+    b = prob.sinograms(imgs, seed)
+    x1, _, _ = prob.sirt(b, 1)
+    x0 = net.forward(x1.view(1, prob.size, prob.size)).view(1, -1)
+    xg, _, _ = prob.sirt(b, iterations, start=x0)
+    g = prob.g
+    ops = fut_ref.SirtOperators(g.angles, g.rhozero, g.deltarho, g.numrhos, prob.size)
+    x64 = ops.iterate(x0.view(-1).cpu().numpy(), b.view(-1).cpu().numpy(), iterations)
+    xg = xg.view(-1).cpu().double().numpy()
+    return {"iterations": iterations, "rel_l2_vs_fp64": float(np.linalg.norm(xg - x64) / np.linalg.norm(x64))}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--train", type=int, default=20000)
+    ap.add_argument("--eval", type=int, default=512)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--angles", type=int, default=180)
+    ap.add_argument("--target-iters", type=int, default=1000)
+    ap.add_argument("--oracle", action="store_true", help="also compare one warm-started solve with the FP64 oracle")
+    ap.add_argument("--sparse-size", type=int, default=512)
+    ap.add_argument("--sparse-angles", type=int, default=90)
+    ap.add_argument("--out", default="")
+    args = ap.parse_args(argv)
+    torch.cuda.set_device(0)
+    log = lambda m: print(m, flush=True)   # noqa: E731
+    prob = Problem(args.size, args.angles)
+    t0 = time.time()
+    xs, ts = make_dataset(prob, args.train, seed=1, target_iters=args.target_iters)
+    torch.cuda.synchronize()
+    t_data = time.time() - t0
+    log(f"dataset {args.train} x {args.size}^2 in {t_data:.1f} s")
+    net = UNet(args.size, args.batch, seed=0)
+    t0 = time.time()
+    hist = train(net, xs, ts, args.epochs, args.batch, args.lr, log=log)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    del xs, ts
+    res = {"train": {"phantoms": args.train, "epochs": args.epochs, "batch": args.batch, "lr": args.lr,
+                     "loss_per_epoch": hist, "data_s": t_data, "train_s": t_train,
+                     "steps": args.epochs * (args.train // args.batch)}}
+    res["eval_dense"] = evaluate(net, prob, args.eval, seed=777777)
+    log(json.dumps(res["eval_dense"]))
+    if args.oracle:
+        res["oracle_check"] = oracle_check(net, prob, seed=777777)
+        log(json.dumps(res["oracle_check"]))
+    sparse = Problem(args.sparse_size, args.sparse_angles)
+    net512 = UNet(args.sparse_size, 8, seed=0)
+    net512.load(net.params())
+    res["eval_sparse_view"] = evaluate(net512, sparse, args.eval, seed=888888)
+    log(json.dumps(res["eval_sparse_view"]))
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump(res, f, indent=1)
+    return res
+
+
+if __name__ == "__main__":
+    main()
