@@ -35,7 +35,7 @@ import numpy as np  # noqa: E402
 
 N_SIZE, N_ANGLES, N_DET = 2048, 2048, 2897     # the projector microbench's dense configuration
 METRIC = "SIRT ms to rel. residual 1e-3: warm-start vs plain, 1 GB300; FP/BP GB/s"
-LEGS = ("proj", "e2e", "sirt", "csr", "cpu")      # default legs; "batch" and "stack" on request
+LEGS = ("proj", "e2e", "sirt", "csr", "cpu")      # default legs; "batch", "stack", "sparse", "unet" on request
 
 
 def set_workload(size, angles, detectors):
@@ -271,7 +271,9 @@ def run_gpu(args, rank, world):
     csr = run_csr_cfg1(dev) if (rank == 0 and "csr" in args.legs) else None
     batch = run_batch_cfg3(dev) if (rank == 0 and "batch" in args.legs) else None
     stack = run_stack_cfg2(dev) if (rank == 0 and "stack" in args.legs) else None
-    return {"step_ms": step_ms, "fp_ms": statistics.median(fp_ms), "bp_ms": statistics.median(bp_ms),
+    sparse = run_sparseview(dev) if (rank == 0 and "sparse" in args.legs) else None
+    unet = run_unet(dev) if (rank == 0 and "unet" in args.legs) else None
+    return {"sparse": sparse, "unet": unet, "step_ms": step_ms, "fp_ms": statistics.median(fp_ms), "bp_ms": statistics.median(bp_ms),
             "wall_s": wall, "clocks": clk.summary(), "e2e": e2e, "sirt": sirt, "csr": csr, "batch": batch,
             "stack": stack,
             "sms": torch.cuda.get_device_properties(dev).multi_processor_count}
@@ -463,6 +465,92 @@ def run_stack_cfg2(dev, nslices=64, iterations=100, seed=0):
             "ms_per_slice_iteration": ms / (nslices * iterations)}
 
 
+def run_sparseview(dev, size=512, detectors=725, counts=(1, 5, 10, 20, 30, 45, 60, 95), reps=20):
+    """The sparse-view programs (forward/backprojection_sparse, datasets of 1 to
+    95 angles in [0, pi)) at N=512, 725 detectors: median microseconds per call
+    and the rate per ray-row step / per (pixel, angle), inputs resident."""
+    import torch
+
+    from synkrotomo_gb300 import phantom
+    from synkrotomo_gb300 import runtime as rt
+
+    img = torch.from_numpy(phantom.ellipse_phantom(size, 0)).to(dev)
+    out = {}
+    for a in counts:
+        g = phantom.geometry(size, a, numrhos=detectors)
+        ang = torch.from_numpy(g.angles).to(dev)
+        sino = torch.rand(a * detectors, device=dev)
+        fo = torch.empty(a * detectors, device=dev)
+        bo = torch.empty(size * size, device=dev)
+        res = {}
+        for name, fn in (("fp", lambda: rt.forwardprojection(ang, g.rhozero, g.deltarho, detectors, img, out=fo,
+                                                             sparse=True)),
+                         ("bp", lambda: rt.backprojection(ang, g.rhozero, g.deltarho, size, sino, out=bo,
+                                                          sparse=True))):
+            for _ in range(3):
+                fn()
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn()
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1) * 1e3)
+            res[name + "_us"] = statistics.median(ts)
+        res["fp_ns_per_ray_row"] = res["fp_us"] * 1e3 / (a * detectors * size)
+        res["bp_ns_per_pixel_angle"] = res["bp_us"] * 1e3 / (size * size * a)
+        out[str(a)] = res
+    return {"size": size, "detectors": detectors, "angles": out}
+
+
+def unet_flops(size, batch):
+    """Tensor-core FLOPs of one U-Net training step (2*H*W*Cin*Cout*9 per 3x3
+    conv and pass): forward, backward-data and backward-weights of the 13
+    convolutions on the tcgen05 engine (the Cin = 1 input conv runs on CUDA
+    cores and is left out; its backward-data pass is not needed)."""
+    from synkrotomo_gb300.unet import LAYERS
+    level = [0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0]
+    fwd = 0.0
+    for (ci, co), lv in zip(LAYERS[1:], level[1:]):
+        hw = (size >> lv) ** 2
+        fwd += 2.0 * hw * batch * ci * co * 9
+    return 3.0 * fwd
+
+
+def run_unet(dev, size=256, batch=32, steps=10):
+    """U-Net warm-starter training step (N=256, batch 32): ms per step and
+    tensor-core TFLOP/s against the measured BF16 peak."""
+    import torch
+
+    from synkrotomo_gb300.unet import UNet
+
+    net = UNet(size, batch, seed=0)
+    g = torch.Generator(device=dev).manual_seed(0)
+    x = torch.rand(batch, size, size, device=dev, generator=g)
+    t = torch.rand(batch, size, size, device=dev, generator=g)
+    for _ in range(3):
+        net.train_step(x, t, lr=1e-4)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        net.train_step(x, t, lr=1e-4)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    fl = unet_flops(size, batch)
+    e0.record()
+    for _ in range(steps):
+        net.forward(x)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / steps
+    return {"size": size, "batch": batch, "ms_per_train_step": ms, "tflops_train": fl / (ms * 1e-3) / 1e12,
+            "ms_forward": fwd_ms, "tflops_forward": fl / 3 / (fwd_ms * 1e-3) / 1e12,
+            "tensor_flops_per_step": fl}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -558,9 +646,16 @@ def main():
             c[k]["frac_hbm"] = c[k]["GB/s"] / hbm
         c["hbm_peak_gbs"] = hbm
         line["csr_cfg1"] = c
-    for key in ("batch", "stack"):
+    for key in ("batch", "stack", "sparse"):
         if res[key] is not None:
-            line[{"batch": "sirt_batch_cfg3", "stack": "sirt_stack_cfg2"}[key]] = res[key]
+            line[{"batch": "sirt_batch_cfg3", "stack": "sirt_stack_cfg2", "sparse": "sparse_view"}[key]] = res[key]
+    if res["unet"] is not None:
+        u = res["unet"]
+        bf16 = float(peaks.get("bf16_tflops", 1900.0))
+        u["frac_train_of_measured_bf16"] = u["tflops_train"] / bf16
+        u["frac_forward_of_measured_bf16"] = u["tflops_forward"] / bf16
+        u["bf16_peak_tflops"] = bf16
+        line["unet_cfg4"] = u
     if "cpu" in args.legs:
         r = cpu_reference_rate(budget_s=10.0)
         cv = step_bytes() / r["step_s"] / 1e9

@@ -5,3 +5,10 @@ Usage as in the reference: ``SIRT.SIRT().main(...).get()``.
 from synkrotomo_gb300.dropin import SIRT
 
 __all__ = ["SIRT"]
+
+if __name__ == "__main__":
+    import sys
+
+    from synkrotomo_gb300.fbench import run_executable
+
+    sys.exit(run_executable("SIRT"))

@@ -160,6 +160,16 @@ int synk_sirt_resident_blocks(void);
 int synk_sirt_batch(synk_context *ctx, int32_t nprob, const synk_sirt_problem *probs, double tol,
                     int32_t grid_blocks);
 
+/* A batched SIRT solve captured once in a CUDA graph (with its own scratch)
+ * and replayed by synk_sirt_plan_launch on the context's stream.  The arrays
+ * of `probs` are bound at creation: change their contents between launches,
+ * not the pointers. */
+typedef struct synk_sirt_plan synk_sirt_plan;
+int synk_sirt_plan_new(synk_context *ctx, synk_sirt_plan **out, int32_t nprob, const synk_sirt_problem *probs,
+                       double tol, int32_t grid_blocks);
+int synk_sirt_plan_launch(synk_context *ctx, synk_sirt_plan *plan);
+void synk_sirt_plan_free(synk_sirt_plan *plan);
+
 /* ---- CSR system matrix (no reference counterpart) ----
  * The forward projector's rule (futhark/forwardprojection.fut:31-56) stored
  * as a sparse matrix A (rows: rays k*numrhos + r, angle-major; columns:
@@ -182,6 +192,27 @@ int synk_csr_spmv_t(synk_context *ctx, const synk_csr *m, const float *y, float 
 /* y[rows] = M x for a caller-owned CSR matrix (int32 row pointers). */
 int synk_spmv_csr32(synk_context *ctx, int64_t rows, const int32_t *rowptr, const int32_t *colidx,
                     const float *vals, const float *x, float *y);
+
+/* ---- the reference's validation programs (futhark/tools/*.fut) ----
+ * One pass over two float32 device arrays of n elements:
+ *   count  = #{ i > 0 : |sane[i] - test[i]| > tol }   (tools/diff.fut:4-6, tol 0.05)
+ *   sse    = sum (sane[i] - test[i])^2, FP64           (tools/mse.fut:2-3)
+ *   all_ok = every |sane[i] - test[i]| < tol           (tools/sanityCheck.fut:3-4)
+ * `out` points to device memory.  synk_diff / synk_mse / synk_sanityCheck
+ * write the reference programs' own results to a device scalar: an int32
+ * count, the float32 mean sse/n and a one-byte boolean; the tolerance is the
+ * programs' std_dev = 0.05. */
+typedef struct {
+    uint64_t count;
+    double sse;
+    int32_t all_ok;
+    int32_t pad_;
+} synk_compare_result;
+int synk_compare(synk_context *ctx, synk_compare_result *out, const float *sane, const float *test, int64_t n,
+                 float tol);
+int synk_diff(synk_context *ctx, int32_t *out, const float *sane, const float *test, int64_t n);
+int synk_mse(synk_context *ctx, float *out, const float *sane, const float *test, int64_t n);
+int synk_sanityCheck(synk_context *ctx, uint8_t *out, const float *sane, const float *test, int64_t n);
 
 /* ---- backprojection that allocates nothing (no counterpart in the reference) ----
  * For callers that cannot let the library allocate device memory: programs

@@ -310,3 +310,32 @@ def relative_residual(A, x, b):
     """||A x - b||_2 / ||b||_2 in FP64."""
     b = np.asarray(b, dtype=np.float64)
     return float(np.linalg.norm(A @ np.asarray(x, np.float64) - b) / np.linalg.norm(b))
+
+
+# --- validation programs (futhark/tools/*.fut) --------------------------------
+# std_dev = 0.05f32 in all three programs (diff.fut:2, sanityCheck.fut:2)
+TOOLS_STD_DEV = np.float32(0.05)
+
+
+def tools_diff(sane, test):
+    """tools/diff.fut:4-6: indices where |s - t| > std_dev get i, the others -1;
+    filter (> 0) keeps the positive ones, so index 0 is never counted."""
+    s = np.asarray(sane, np.float32)
+    t = np.asarray(test, np.float32)
+    d = np.abs(s - t)                          # f32 arithmetic, as the program
+    marks = np.where(d > TOOLS_STD_DEV, np.arange(s.size), -1)
+    return np.int32(np.count_nonzero(marks > 0))
+
+
+def tools_mse(sane, test):
+    """tools/mse.fut:2-3: sum of (s - t)**2 divided by n (evaluated in FP64)."""
+    s = np.asarray(sane, np.float64)
+    t = np.asarray(test, np.float64)
+    return float(np.sum((s - t) ** 2) / s.size)
+
+
+def tools_sanity(sane, test):
+    """tools/sanityCheck.fut:3-4: every |s - t| < std_dev."""
+    s = np.asarray(sane, np.float32)
+    t = np.asarray(test, np.float32)
+    return bool(np.all(np.abs(s - t) < TOOLS_STD_DEV))

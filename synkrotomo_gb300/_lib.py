@@ -89,6 +89,10 @@ SIGNATURES = {
     "synk_sirt_resident_blocks": (ctypes.c_int, []),
     "synk_sirt_batch": (ctypes.c_int, [c_ctx, ctypes.c_int32, ctypes.POINTER(SynkProblem), ctypes.c_double,
                                        ctypes.c_int32]),
+    "synk_sirt_plan_new": (ctypes.c_int, [c_ctx, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                          ctypes.POINTER(SynkProblem), ctypes.c_double, ctypes.c_int32]),
+    "synk_sirt_plan_launch": (ctypes.c_int, [c_ctx, ctypes.c_void_p]),
+    "synk_sirt_plan_free": (None, [ctypes.c_void_p]),
     "synk_csr_new": (ctypes.c_int, [c_ctx, ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.c_int64,
                                     ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_int32]),
     "synk_csr_free": (None, [ctypes.c_void_p]),
@@ -119,6 +123,11 @@ SIGNATURES = {
     "synk_unet_train_step": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                             ctypes.c_float, ctypes.c_int32, ctypes.c_void_p]),
     "synk_unet_gradients": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p]),
+    "synk_compare": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_float]),
+    "synk_diff": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "synk_mse": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "synk_sanityCheck": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
     "synk_backprojection_noalloc": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                                    ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_void_p,
                                                    ctypes.c_int64]),

@@ -4,8 +4,8 @@
 // A block of 256 threads owns a tile of 32 columns; thread (lane, warp) owns
 // column lane and PIX rows spaced RSTEP apart.  The per-angle constants of
 // the chord-length trapezoid are staged in shared memory 64 angles at a time
-// and read as one broadcast float4 + one float per angle; each (pixel, angle)
-// then costs ~16 FP32/INT instructions and two sinogram gathers:
+// and read as one broadcast float4 + one float2 per angle; each (pixel, angle)
+// then costs ~14 FP32/INT instructions and two sinogram gathers:
 //   q    = x_c*cos - y_c*sin - rhozero            (rho of the centre, shifted)
 //   s0   = ceil((q - sqrt(2)/2) / deltarho)       (first candidate detector)
 //   d_i  = s0*deltarho + i*deltarho - q           (signed distance ray -> centre)
@@ -25,7 +25,7 @@ constexpr int kBpChunk = 64;
 
 struct BpStage {
     float4 cs[kBpChunk];   // cos, sin, h/b, 1/b
-    float lb[kBpChunk];    // lbase
+    float2 le[kBpChunk];   // lbase, h/b - (1 - sqrt(2)/2)/b
 };
 
 // Stages angles [k0, k0 + kBpChunk) of P (all threads of the block call it).
@@ -33,23 +33,30 @@ __device__ __forceinline__ void bp_stage(const ProbGeom &P, int k0, BpStage &st)
     for (int i = threadIdx.x; i < kBpChunk; i += blockDim.x) {
         const int k = k0 + i;
         float4 v = make_float4(0.0f, 0.0f, -1.0f, 0.0f);   // zero weight
-        float l = 0.0f;
+        float2 l = make_float2(0.0f, -1.0f);
         if (k < P.a) {
             const AngleGeom g = load_geom(P.geom, k);
             if (!g.exact) {
                 v = make_float4(g.c, g.s, g.h_over_b, g.inv_b);
-                l = g.lbase;
+                l = make_float2(g.lbase, fmaf(-(1.0f - fact_f32()), g.inv_b, g.h_over_b));
             }
         }
         st.cs[i] = v;
-        st.lb[i] = l;
+        st.le[i] = l;
     }
 }
 
-// Accumulates angles k in [k0, k1) with (k - k0) % kstride == kphase of the
-// staged chunk (chunk starts at kc) into acc[m] for the PIX pixels
-// (row0 + m*RSTEP, col).  sino: the problem's sinogram [a][D].
-template <int PIX, bool RPP2>
+// Accumulates angles k in [kc, kend) with (k - kc) % kstride == kphase of the
+// staged chunk into acc[m] for the PIX pixels (row0 + m*ystep, col) whose
+// centres are (xc, yc0 + m*ystep).  sino: the problem's sinogram [a][D].
+//
+// UNIT (deltarho = 1): with q = rho_c - rhozero - sqrt(2)/2, the first
+// candidate detector is s0 = ceil(q) and e = s0 - q is in [0, 1); the two
+// candidates sit at signed distances e - sqrt(2)/2 and e + 1 - sqrt(2)/2
+// from the centre (the second is never negative), so
+//   w0 = sat(h/b - |e - sqrt(2)/2| / b),  w1 = sat(c1 - e/b),  c1 = h/b - (1 - sqrt(2)/2)/b.
+// INRANGE: the host proved that every window [s0, s0+1] lies in [0, D).
+template <int PIX, bool UNIT, bool INRANGE>
 __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, int kc, int kend, int kphase,
                                          int kstride, const float *__restrict__ sino, float xc, float yc0,
                                          float ystep, float (&acc)[PIX]) {
@@ -57,42 +64,68 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
     const int D = P.D;
     const unsigned uD = (unsigned)D;
     const int nk = min(kBpChunk, kend - kc);
+    const float zoff = -P.rhozero - fact;
     for (int i = kphase; i < nk; i += kstride) {
         const float4 g = st.cs[i];
-        const float lb = st.lb[i];
+        const float2 le = st.le[i];
         const float *__restrict__ row = sino + (size_t)(kc + i) * D;
-        // q for the first pixel, then step along the column
-        float t = fmaf(-yc0, g.y, -P.rhozero);
-        const float tstep = -ystep * g.y;
+        if constexpr (UNIT) {
+            float q = fmaf(xc, g.x, fmaf(-yc0, g.y, zoff));
+            const float dq = -ystep * g.y;
 #pragma unroll
-        for (int m = 0; m < PIX; ++m, t += tstep) {
-            const float q = fmaf(xc, g.x, t);
-            int s0;
-            float s0f;
-            if (RPP2) {
-                s0f = ceil_magic(q - fact, s0);
-            } else {
-                s0f = ceil_magic((q - fact) * P.inv_deltarho, s0);
-                s0f = s0f * P.deltarho;
+            for (int m = 0; m < PIX; ++m) {
+                if (m) q += dq;
+                int s0;
+                const float e = ceil_magic(q, s0) - q;
+                const float w0 = __saturatef(fmaf(-fabsf(e - fact), g.w, g.z));
+                const float w1 = __saturatef(fmaf(-e, g.w, le.y));
+                float v0, v1;
+                if constexpr (INRANGE) {
+                    const float *p = row + s0;
+                    v0 = __ldg(p);
+                    v1 = __ldg(p + 1);
+                } else {
+                    v0 = ((unsigned)s0 < uD) ? __ldg(row + s0) : 0.0f;
+                    v1 = ((unsigned)(s0 + 1) < uD) ? __ldg(row + s0 + 1) : 0.0f;
+                }
+                acc[m] = fmaf(le.x, fmaf(w1, v1, w0 * v0), acc[m]);
             }
-            float d = s0f - q;
-            float a = 0.0f;
-            if (RPP2) {
-                const float w0 = __saturatef(fmaf(-fabsf(d), g.w, g.z));
-                const float w1 = __saturatef(fmaf(-fabsf(d + 1.0f), g.w, g.z));
-                const float v0 = ((unsigned)s0 < uD) ? __ldg(row + s0) : 0.0f;
-                const float v1 = ((unsigned)(s0 + 1) < uD) ? __ldg(row + s0 + 1) : 0.0f;
-                a = fmaf(w1, v1, w0 * v0);
-            } else {
+        } else {
+            float t = fmaf(-yc0, g.y, -P.rhozero);
+            const float tstep = -ystep * g.y;
+#pragma unroll
+            for (int m = 0; m < PIX; ++m, t += tstep) {
+                const float qc = fmaf(xc, g.x, t);             // rho_c - rhozero
+                int s0;
+                float s0f = ceil_magic((qc - fact) * P.inv_deltarho, s0);
+                float d = s0f * P.deltarho - qc;
+                float a = 0.0f;
                 for (int q2 = 0; q2 < P.rpp; ++q2, d += P.deltarho) {
                     const int det = s0 + q2;
                     const float w = __saturatef(fmaf(-fabsf(d), g.w, g.z));
                     if ((unsigned)det < uD) a = fmaf(w, __ldg(row + det), a);
                 }
+                acc[m] = fmaf(le.x, a, acc[m]);
             }
-            acc[m] = fmaf(lb, a, acc[m]);
         }
     }
+}
+
+// True when every pixel's two candidate detectors of the UNIT path lie in
+// [0, D) (deltarho = 1 and a detector row covering the image's circumcircle,
+// as the reference's D >= ceil(N*sqrt(2)) with centred rhozero does).  The
+// tiles cover rows and columns [0, 32*ceil(N/32)), so the bound takes the
+// padded extent, and it keeps a margin for the float rounding of q.
+inline bool bp_windows_in_range(const ProbGeom &P) {
+    if (P.deltarho != 1.0f) return false;
+    const int ext = (P.N + 31) / 32 * 32;
+    const double m = fmax(P.half - 0.5, ext - 0.5 - P.half);       // max |x_c|, |y_c| of a tile pixel
+    const double R = m * 1.4142135623730951;                         // max |rho_c|
+    const double f = 0.70710677;
+    const double rz = (double)P.rhozero;
+    const double margin = 1e-2 + 1e-5 * (R + fabs(rz));
+    const double lo = -R - f - rz, hi = R - f - rz;
+    return ceil(lo - margin) >= 0.0 && ceil(hi + margin) + 1.0 <= (double)P.D - 1.0;
 }
 
 // The near-axis angles of list[0..nexact) for the PIX pixels, the reference's

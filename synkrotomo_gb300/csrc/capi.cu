@@ -15,6 +15,7 @@
 #include "sirt_internal.cuh"
 #include "csr_internal.cuh"
 #include "fp_tile.cuh"
+#include "bp_tile.cuh"
 #include "umma_gemm.cuh"
 #include "unet.cuh"
 
@@ -225,7 +226,11 @@ int pick_bp_split(long long tasks, long long resident_warps, int64_t a) {
 
 int valid_split(int s) { return s == 1 || s == 2 || s == 4 || s == 8; }
 
-int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double tol, int grid_blocks) {
+// `staging`: optional pinned host buffer of nprob SirtProblem entries; the
+// problem table is uploaded from it (a copy a CUDA graph can capture) instead
+// of from pageable memory.
+int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double tol, int grid_blocks,
+               void *staging = nullptr) {
     int rc;
     if (nprob < 1 || nprob > (1 << 16)) return fail(ctx, SYNK_EINVAL, "bad problem count %d", nprob);
     if (!in) return fail(ctx, SYNK_EINVAL, "null problem table");
@@ -315,6 +320,7 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         const long long fp_tasks = (long long)q.nslices * q.numrhos * ((q.a + 31) / 32);
         const long long bp_tasks = (long long)q.nslices * ((q.size + 3) / 4) * ((q.size + 31) / 32);
         const long long share = nprob > 1 ? resident_warps / nprob + 1 : resident_warps;
+        h.bp_inrange = bp_windows_in_range(h.P) ? 1 : 0;
         h.fp_split = q.fp_split ? q.fp_split : pick_fp_split(fp_tasks, share, q.size);
         h.bp_split = q.bp_split ? q.bp_split : pick_bp_split(bp_tasks, share, q.a);
         h.fp_ips = h.bp_ips = 0;
@@ -336,10 +342,17 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
     SYNK_CUDA(sc.get(&dprobs, (size_t)nprob), "cudaMallocAsync(problem table)");
     SYNK_CUDA(sc.get(&totals, 2), "cudaMallocAsync");
     SYNK_CUDA(sc.get(&words, 8), "cudaMallocAsync");
-    // from pageable memory: the copy is staged before the call returns, so the
-    // host vector may go out of scope afterwards
-    SYNK_CUDA(cudaMemcpyAsync(dprobs, sorted.data(), sizeof(SirtProblem) * nprob, cudaMemcpyHostToDevice, st),
-              "upload problem table");
+    if (staging) {
+        // pinned copy: stays valid for every replay of a captured graph
+        memcpy(staging, sorted.data(), sizeof(SirtProblem) * nprob);
+        SYNK_CUDA(cudaMemcpyAsync(dprobs, staging, sizeof(SirtProblem) * nprob, cudaMemcpyHostToDevice, st),
+                  "upload problem table");
+    } else {
+        // from pageable memory: the copy is staged before the call returns, so
+        // the host vector may go out of scope afterwards
+        SYNK_CUDA(cudaMemcpyAsync(dprobs, sorted.data(), sizeof(SirtProblem) * nprob, cudaMemcpyHostToDevice, st),
+                  "upload problem table");
+    }
     SYNK_CUDA(cudaMemsetAsync(words, 0, sizeof(unsigned) * 8, st), "memset");
     SYNK_CUDA(launch_sirt_plan(dprobs, nprob, totals, st), "plan kernel");
     SirtParams sp;
@@ -500,6 +513,78 @@ int synk_SIRT3D(synk_context *ctx, float *out, const float *angles, int64_t a, c
 }
 
 int synk_sirt_resident_blocks(void) { return sirt_persistent_grid(nullptr); }
+
+struct synk_sirt_plan {
+    int device = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void *staging = nullptr;
+};
+
+static void plan_release(synk_sirt_plan *p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->staging) cudaFreeHost(p->staging);
+    delete p;
+}
+
+int synk_sirt_plan_new(synk_context *ctx, synk_sirt_plan **out, int32_t nprob, const synk_sirt_problem *probs,
+                       double tol, int32_t grid_blocks) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out) return fail(ctx, SYNK_EINVAL, "null pointer");
+    *out = nullptr;
+    if (nprob < 1 || nprob > (1 << 16) || !probs) return fail(ctx, SYNK_EINVAL, "bad problem table");
+    synk_sirt_plan *plan = new synk_sirt_plan();
+    plan->device = ctx->device;
+    cudaError_t e = cudaHostAlloc(&plan->staging, sizeof(SirtProblem) * (size_t)nprob, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        plan_release(plan);
+        return cuda_fail(ctx, e, "cudaHostAlloc(problem table)");
+    }
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) {
+        plan_release(plan);
+        return cuda_fail(ctx, e, "cudaStreamCreate");
+    }
+    cudaStream_t saved = ctx->stream;
+    ctx->stream = cs;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) rc = sirt_batch(ctx, nprob, probs, tol, grid_blocks, plan->staging);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(cs, &g) : e;
+    ctx->stream = saved;
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess || e2 != cudaSuccess || rc != SYNK_OK) {
+        if (g) cudaGraphDestroy(g);
+        plan_release(plan);
+        if (rc != SYNK_OK) return rc;
+        return cuda_fail(ctx, e != cudaSuccess ? e : e2, "stream capture of the SIRT solve");
+    }
+    plan->graph = g;
+    if ((e = cudaGraphInstantiate(&plan->exec, g, 0)) != cudaSuccess) {
+        plan_release(plan);
+        return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    *out = plan;
+    return SYNK_OK;
+}
+
+int synk_sirt_plan_launch(synk_context *ctx, synk_sirt_plan *plan) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!plan || !plan->exec) return fail(ctx, SYNK_EINVAL, "null plan");
+    SYNK_CUDA(cudaGraphLaunch(plan->exec, ctx->stream), "cudaGraphLaunch");
+    return SYNK_OK;
+}
+
+void synk_sirt_plan_free(synk_sirt_plan *plan) {
+    if (!plan) return;
+    cudaSetDevice(plan->device);
+    cudaDeviceSynchronize();
+    plan_release(plan);
+}
 
 int synk_sirt_batch(synk_context *ctx, int32_t nprob, const synk_sirt_problem *probs, double tol,
                     int32_t grid_blocks) {
@@ -758,6 +843,52 @@ int synk_spmv_csr32(synk_context *ctx, int64_t rows, const int32_t *rowptr, cons
     if (!rowptr || !colidx || !vals || !x || !y) return fail(ctx, SYNK_EINVAL, "null pointer");
     SYNK_CUDA(launch_spmv(rows, nullptr, rowptr, colidx, vals, x, y, ctx->stream), "spmv kernel");
     return SYNK_OK;
+}
+
+int synk_compare(synk_context *ctx, synk_compare_result *out, const float *sane, const float *test, int64_t n,
+                 float tol) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (n < 0) return fail(ctx, SYNK_EINVAL, "negative length");
+    if (!out || (n && (!sane || !test))) return fail(ctx, SYNK_EINVAL, "null pointer");
+    SYNK_CUDA(launch_compare(sane, test, n, tol, out, ctx->stream), "compare kernel");
+    return SYNK_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// tools/diff.fut, mse.fut and sanityCheck.fut share std_dev = 0.05f32.
+constexpr float kToolsStdDev = 0.05f;
+
+int compare_program(synk_context *ctx, int what, void *out, const float *sane, const float *test, int64_t n) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (n < 0) return fail(ctx, SYNK_EINVAL, "negative length");
+    if (!out || (n && (!sane || !test))) return fail(ctx, SYNK_EINVAL, "null pointer");
+    Scratch scr(ctx->stream);
+    CompareResult *r = nullptr;
+    SYNK_CUDA(scr.get(&r, 1), "scratch");
+    SYNK_CUDA(launch_compare(sane, test, n, kToolsStdDev, r, ctx->stream), "compare kernel");
+    SYNK_CUDA(launch_compare_finish(r, n, what, out, ctx->stream), "compare kernel");
+    return SYNK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int synk_diff(synk_context *ctx, int32_t *out, const float *sane, const float *test, int64_t n) {
+    return compare_program(ctx, 0, out, sane, test, n);
+}
+
+int synk_mse(synk_context *ctx, float *out, const float *sane, const float *test, int64_t n) {
+    return compare_program(ctx, 1, out, sane, test, n);
+}
+
+int synk_sanityCheck(synk_context *ctx, uint8_t *out, const float *sane, const float *test, int64_t n) {
+    return compare_program(ctx, 2, out, sane, test, n);
 }
 
 }  // extern "C"

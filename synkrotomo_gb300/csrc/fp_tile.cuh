@@ -65,22 +65,30 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
     const float slope = g.slope, ainv = g.ainv;
     const int stride = P.N + 2;
     const unsigned lim = (unsigned)P.N;     // c + 1 in [0, N]
+    // u of rows j..j+3 from one float row counter: u0 + k*slope per lane
+    const float u1 = u0 + slope, u2 = u0 + 2.0f * slope, u3 = u0 + 3.0f * slope;
     float sum = 0.0f, comp = 0.0f;
+    auto row = [&](float u, int jrow, float &part) {
+        int c;
+        const float fl = floor_magic(u, c);
+        const float t = right_share(u, fl, ainv);
+        const bool ok = (unsigned)(c + 1) <= lim;
+        const float *p = img_pad + (jrow * stride + c + 1);
+        const float v0 = ok ? __ldg(p) : 0.0f;
+        const float v1 = ok ? __ldg(p + 1) : 0.0f;
+        part += fmaf(t, v1 - v0, v0);
+    };
     for (int j = J0; j < J1;) {
         const int jend = min(j + 32, J1);
         float part = 0.0f;
-#pragma unroll 4
-        for (; j < jend; ++j) {
-            const float u = fmaf((float)j, slope, u0);
-            int c;
-            const float fl = floor_magic(u, c);
-            const float t = right_share(u, fl, ainv);
-            const bool ok = (unsigned)(c + 1) <= lim;
-            const float *p = img_pad + (j * stride + c + 1);
-            const float v0 = ok ? __ldg(p) : 0.0f;
-            const float v1 = ok ? __ldg(p + 1) : 0.0f;
-            part += fmaf(t, v1 - v0, v0);
+        float jf = (float)j;
+        for (; j + 3 < jend; j += 4, jf += 4.0f) {
+            row(fmaf(jf, slope, u0), j, part);
+            row(fmaf(jf, slope, u1), j + 1, part);
+            row(fmaf(jf, slope, u2), j + 2, part);
+            row(fmaf(jf, slope, u3), j + 3, part);
         }
+        for (; j < jend; ++j, jf += 1.0f) row(fmaf(jf, slope, u0), j, part);
         comp_add(sum, comp, part);
     }
     return k >= 0 ? (sum + comp) * g.lbase : 0.0f;

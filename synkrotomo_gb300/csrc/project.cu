@@ -201,7 +201,7 @@ cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad,
 
 // ---- backprojection ---------------------------------------------------------------
 
-template <bool UNIT>
+template <bool UNIT, bool INRANGE>
 __global__ void __launch_bounds__(256) bp_tile_kernel(ProbGeom P, AngleLists L, const float *__restrict__ sino,
                                                       float *__restrict__ out) {
     __shared__ BpStage st;
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(256) bp_tile_kernel(ProbGeom P, AngleLists L, 
         bp_stage(P, kc, st);
         __syncthreads();
         float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        bp_chunk<4, UNIT>(P, st, kc, P.a, 0, 1, sino, xc, yc0, 8.0f, part);
+        bp_chunk<4, UNIT, INRANGE>(P, st, kc, P.a, 0, 1, sino, xc, yc0, 8.0f, part);
 #pragma unroll
         for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], part[m]);
     }
@@ -231,8 +231,9 @@ __global__ void __launch_bounds__(256) bp_tile_kernel(ProbGeom P, AngleLists L, 
 
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream) {
     dim3 grid((P.N + 31) / 32, (P.N + 31) / 32);
-    if (P.deltarho == 1.0f) bp_tile_kernel<true><<<grid, 256, 0, stream>>>(P, L, sino, img);
-    else bp_tile_kernel<false><<<grid, 256, 0, stream>>>(P, L, sino, img);
+    if (bp_windows_in_range(P)) bp_tile_kernel<true, true><<<grid, 256, 0, stream>>>(P, L, sino, img);
+    else if (P.deltarho == 1.0f) bp_tile_kernel<true, false><<<grid, 256, 0, stream>>>(P, L, sino, img);
+    else bp_tile_kernel<false, false><<<grid, 256, 0, stream>>>(P, L, sino, img);
     return cudaGetLastError();
 }
 

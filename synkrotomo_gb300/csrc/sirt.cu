@@ -243,14 +243,16 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
         const float yc0 = (float)(row0 - P.half) + 0.5f;
         const float *rr = q.rr + (size_t)s * pr;
         const bool unit = P.deltarho == 1.0f;
+        const bool inrange = q.bp_inrange != 0;
         float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f}, comp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         for (int kc = 0; kc < P.a; kc += kBpChunk) {
             __syncthreads();
             bp_stage(P, kc, sh.st);
             __syncthreads();
             float prt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            if (unit) bp_chunk<4, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
-            else bp_chunk<4, false>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            if (inrange) bp_chunk<4, true, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            else if (unit) bp_chunk<4, true, false>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            else bp_chunk<4, false, false>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
 #pragma unroll
             for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], prt[m]);
         }

@@ -25,6 +25,7 @@ struct SirtProblem {
     int iterations;
     int fp_split;         // 1,2,4,8 warps share one ray (rows split)
     int bp_split;         // 1,2,4,8 warps share one pixel (angles split)
+    int bp_inrange;       // every pixel's detector window is inside the sinogram (no bounds checks)
     // filled on the device by sirt_plan_kernel (they depend on the angle lists)
     int fp_ips;           // FP work items per slice
     int bp_ips;           // BP work items per slice

@@ -306,4 +306,11 @@ cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad,
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream);
 cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, cudaStream_t stream);
 
+// compare.cu: the validation programs (diff, mse, sanityCheck) in one pass.
+typedef synk_compare_result CompareResult;
+cudaError_t launch_compare(const float *sane, const float *test, long long n, float tol, CompareResult *out,
+                           cudaStream_t stream);
+// what: 0 = int32 count (diff), 1 = float32 sse/n (mse), 2 = uint8 all_ok (sanityCheck)
+cudaError_t launch_compare_finish(const CompareResult *r, long long n, int what, void *dst, cudaStream_t stream);
+
 }  // namespace synk

@@ -114,3 +114,40 @@ class SIRT3D(_Entry):
 
 def _np(x):
     return np.asarray(x)
+
+
+class _Compare(_Entry):
+    """The reference's validation programs (futhark/tools/*.fut): main(sane, test)
+    on two float32 arrays of one length, returning a scalar as Futhark's
+    generated classes do for scalar results."""
+
+    _program = ""
+
+    def main(self, sane, test):
+        with torch.cuda.device(self.device):
+            s = rt.to_device_f32(sane, 0, "sane", self.device)
+            t = rt.to_device_f32(test, 1, "test", self.device)
+            if s.numel() != t.numel():
+                raise ValueError(f"{self._program}: sane has {s.numel()} elements and test {t.numel()}")
+            return rt.compare_program(self._program, s, t)
+
+
+class diff(_Compare):
+    """futhark/tools/diff.fut: the number of indices i > 0 with |sane-test| > 0.05 (i32)."""
+
+    entry_points = {"main": (["[]f32", "[]f32"], ["i32"])}
+    _program = "diff"
+
+
+class mse(_Compare):
+    """futhark/tools/mse.fut: the mean squared difference (f32)."""
+
+    entry_points = {"main": (["[]f32", "[]f32"], ["f32"])}
+    _program = "mse"
+
+
+class sanityCheck(_Compare):
+    """futhark/tools/sanityCheck.fut: whether every |sane-test| < 0.05 (bool)."""
+
+    entry_points = {"main": (["[]f32", "[]f32"], ["bool"])}
+    _program = "sanityCheck"

@@ -271,6 +271,36 @@ def sirt_batch(problems: list, tol: float = 0.0, grid_blocks: int = 0) -> list:
     return problems
 
 
+class SirtPlan:
+    """A batched SIRT solve captured in a CUDA graph (``synk_sirt_plan_*``).
+
+    The problems' tensors are bound at creation; refill them in place and call
+    ``launch()`` to solve again."""
+
+    def __init__(self, problems: list, tol: float = 0.0, grid_blocks: int = 0):
+        self.problems = problems
+        self.ctx = context(problems[0].projections.device.index)
+        arr = (_lib.SynkProblem * len(problems))(*[p._desc() for p in problems])
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.synk_sirt_plan_new(self.ctx.handle, ctypes.byref(h), len(problems), arr,
+                                                       float(tol), int(grid_blocks)), "synk_sirt_plan_new")
+        self._h = h
+
+    def launch(self):
+        ctx = context(self.ctx.device)
+        ctx.check(ctx.lib.synk_sirt_plan_launch(ctx.handle, self._h), "synk_sirt_plan_launch")
+        return self.problems
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self.ctx.lib.synk_sirt_plan_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+
 def sirt(angles: torch.Tensor, rhozero: float, deltarho: float, image: torch.Tensor, projections: torch.Tensor,
          iterations: int, out: torch.Tensor | None = None) -> torch.Tensor:
     """``iterations`` SIRT updates from ``image`` (futhark/SIRT.fut:43-49)."""
@@ -293,6 +323,38 @@ def sirt3d(angles: torch.Tensor, rhos: torch.Tensor, projections: torch.Tensor, 
                              _ptr(projections), projections.numel(), int(iterations), int(size))
     ctx.check(rc, "SIRT3D")
     return out
+
+
+def compare(sane: torch.Tensor, test: torch.Tensor, tol: float = 0.05) -> tuple:
+    """(count, sse, all_ok) of futhark/tools/{diff,mse,sanityCheck}.fut in one
+    pass: the indices i > 0 with |sane-test| > tol, the FP64 sum of squared
+    differences, and whether every |sane-test| < tol."""
+    if sane.numel() != test.numel():
+        raise ValueError(f"compare: lengths differ ({sane.numel()} vs {test.numel()})")
+    ctx = context(sane.device.index)
+    res = torch.empty(3, dtype=torch.float64, device=sane.device)   # 24 B: synk_compare_result
+    rc = ctx.lib.synk_compare(ctx.handle, _ptr(res), _ptr(sane), _ptr(test), sane.numel(), float(tol))
+    ctx.check(rc, "compare")
+    raw = res.cpu().numpy().view(np.uint8)
+    count = int(raw[:8].view(np.uint64)[0])
+    sse = float(raw[8:16].view(np.float64)[0])
+    ok = bool(raw[16:20].view(np.int32)[0])
+    return count, sse, ok
+
+
+def compare_program(name: str, sane: torch.Tensor, test: torch.Tensor):
+    """The result of tools/diff.fut (np.int32), mse.fut (np.float32) or
+    sanityCheck.fut (np.bool_), computed on the GPU."""
+    if sane.numel() != test.numel():
+        raise ValueError(f"{name}: lengths differ ({sane.numel()} vs {test.numel()})")
+    ctx = context(sane.device.index)
+    kind = {"diff": (ctx.lib.synk_diff, torch.int32), "mse": (ctx.lib.synk_mse, torch.float32),
+            "sanityCheck": (ctx.lib.synk_sanityCheck, torch.uint8)}
+    fn, dt = kind[name]
+    out = torch.empty(1, dtype=dt, device=sane.device)
+    ctx.check(fn(ctx.handle, _ptr(out), _ptr(sane), _ptr(test), sane.numel()), name)
+    v = out.cpu().numpy()[0]
+    return np.bool_(v != 0) if name == "sanityCheck" else v
 
 
 def image_side(n: int) -> int:

@@ -125,29 +125,28 @@ def first_below(hist: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
     return k
 
 
-def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 100, 200), max_iters: int = 600):
+def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 100, 200), max_iters: int = 600,
+             abs_targets=()):
     """Plain zero-start SIRT vs warm-started SIRT on n held-out images.
 
     For each plain budget K: r*_i = 1.01 x the residual plain SIRT reaches on
-    image i after K iterations; iterations to r*_i come from full residual
-    histories (plain and warm, one run each).  Milliseconds are measured on
-    batched runs that stop at the loosest r* of the batch (one stopping level
-    per launch), the warm run including the normalised backprojection and
-    the network."""
-    K = max(budgets)
+    image i after K iterations.  For each absolute target r (abs_targets, e.g.
+    1e-3 on noise-free data): r*_i = r.  Iterations to r*_i come from full
+    residual histories (plain and warm, one run each, max_iters iterations;
+    an image that never reaches r*_i counts max_iters and is reported).
+    Milliseconds are measured on batched runs that stop each image at its own
+    r*_i when r* is absolute, and at the loosest r* of the batch otherwise; the
+    warm run includes the normalised backprojection and the network."""
+    plain_len = max(max(budgets) if budgets else 0, max_iters if abs_targets else 0)
     imgs = ellipse_batch(n, prob.size, seed)
     b = prob.sinograms(imgs, seed)
-    _, hp, _ = prob.sirt(b, K, residuals=True)
+    _, hp, _ = prob.sirt(b, plain_len, residuals=True)
     x1, _, _ = prob.sirt(b, 1)
     x0 = net.forward(x1.view(n, prob.size, prob.size)).view(n, -1)
     _, hw, _ = prob.sirt(b, max_iters, start=x0, residuals=True)
     fallback = hw[:, 0] > 1.0          # the warm start is worse than the zero start
-    rows = []
-    for Kb in budgets:
-        rstar = hp[:, Kb] * 1.01
-        it_plain = first_below(hp, rstar).float()
-        it_warm = torch.where(fallback, it_plain, first_below(hw, rstar).float())
-        tol = float(rstar.max().item())
+
+    def timed(tol):
         ms = {}
         for label in ("plain", "warm"):
             for rep in range(2):                       # first run warms up
@@ -162,16 +161,33 @@ def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 1
                 t1.record()
                 torch.cuda.synchronize()
             ms[label] = t0.elapsed_time(t1)
-        rows.append({"budget": Kb, "target_residual_mean": float(rstar.mean().item()),
-                     "plain_iterations_mean": float(it_plain.mean().item()),
-                     "warm_iterations_mean": float(it_warm.mean().item()),
-                     "speedup_iterations": float(it_plain.mean().item() / max(it_warm.mean().item(), 1e-9)),
-                     "batched_ms_plain": ms["plain"], "batched_ms_warm": ms["warm"],
-                     "speedup_ms": ms["plain"] / max(ms["warm"], 1e-9)})
-    return {"n": n, "size": prob.size, "angles": prob.n_angles,
+        return ms
+
+    def row(rstar, tol):
+        it_plain = first_below(hp, rstar).float()
+        it_warm = torch.where(fallback, it_plain, first_below(hw, rstar).float())
+        ms = timed(tol)
+        return {"target_residual_mean": float(rstar.mean().item()),
+                "plain_iterations_mean": float(it_plain.mean().item()),
+                "warm_iterations_mean": float(it_warm.mean().item()),
+                "plain_iterations_median": float(it_plain.median().item()),
+                "warm_iterations_median": float(it_warm.median().item()),
+                "plain_not_reached": int((it_plain >= hp.shape[1]).sum().item()),
+                "warm_not_reached": int((it_warm >= hw.shape[1]).sum().item()),
+                "speedup_iterations": float(it_plain.mean().item() / max(it_warm.mean().item(), 1e-9)),
+                "batched_ms_plain": ms["plain"], "batched_ms_warm": ms["warm"],
+                "speedup_ms": ms["plain"] / max(ms["warm"], 1e-9)}
+
+    rows = []
+    for Kb in budgets:
+        rstar = hp[:, Kb] * 1.01
+        rows.append({"budget": Kb, **row(rstar, float(rstar.max().item()))})
+    for r in abs_targets:
+        rows.append({"residual": float(r), **row(torch.full_like(hp[:, 0], float(r)), float(r))})
+    return {"n": n, "size": prob.size, "angles": prob.n_angles, "noise": prob.noise,
             "warm_start_residual_mean": float(hw[:, 0].mean().item()),
             "plain_residual_after_1": float(hp[:, 1].mean().item()),
-            "fallback_images": int(fallback.sum().item()), "budgets": rows}
+            "fallback_images": int(fallback.sum().item()), "rows": rows}
 
 
 def oracle_check(net: UNet, prob: Problem, seed: int, iterations: int = 30) -> dict:
@@ -201,13 +217,19 @@ def main(argv=None):
     ap.add_argument("--angles", type=int, default=180)
     ap.add_argument("--target-iters", type=int, default=1000)
     ap.add_argument("--oracle", action="store_true", help="also compare one warm-started solve with the FP64 oracle")
+    ap.add_argument("--noise", type=float, default=0.01, help="Gaussian noise, fraction of each sinogram's max")
+    ap.add_argument("--budgets", default="10,20,50,100,200", help="plain budgets K (r* = 1.01 r_plain(K))")
+    ap.add_argument("--abs-targets", default="", help="absolute residual targets, e.g. 1e-3 (noise-free data)")
+    ap.add_argument("--max-iters", type=int, default=600)
     ap.add_argument("--sparse-size", type=int, default=512)
     ap.add_argument("--sparse-angles", type=int, default=90)
     ap.add_argument("--out", default="")
     args = ap.parse_args(argv)
     torch.cuda.set_device(0)
     log = lambda m: print(m, flush=True)   # noqa: E731
-    prob = Problem(args.size, args.angles)
+    budgets = tuple(int(v) for v in args.budgets.split(",") if v)
+    abs_t = tuple(float(v) for v in args.abs_targets.split(",") if v)
+    prob = Problem(args.size, args.angles, noise=args.noise)
     t0 = time.time()
     xs, ts = make_dataset(prob, args.train, seed=1, target_iters=args.target_iters)
     torch.cuda.synchronize()
@@ -219,18 +241,20 @@ def main(argv=None):
     torch.cuda.synchronize()
     t_train = time.time() - t0
     del xs, ts
-    res = {"train": {"phantoms": args.train, "epochs": args.epochs, "batch": args.batch, "lr": args.lr,
+    res = {"train": {"phantoms": args.train, "noise": args.noise, "target_iters": args.target_iters, "epochs": args.epochs, "batch": args.batch, "lr": args.lr,
                      "loss_per_epoch": hist, "data_s": t_data, "train_s": t_train,
                      "steps": args.epochs * (args.train // args.batch)}}
-    res["eval_dense"] = evaluate(net, prob, args.eval, seed=777777)
+    res["eval_dense"] = evaluate(net, prob, args.eval, seed=777777, budgets=budgets, max_iters=args.max_iters,
+                                 abs_targets=abs_t)
     log(json.dumps(res["eval_dense"]))
     if args.oracle:
         res["oracle_check"] = oracle_check(net, prob, seed=777777)
         log(json.dumps(res["oracle_check"]))
-    sparse = Problem(args.sparse_size, args.sparse_angles)
+    sparse = Problem(args.sparse_size, args.sparse_angles, noise=args.noise)
     net512 = UNet(args.sparse_size, 8, seed=0)
     net512.load(net.params())
-    res["eval_sparse_view"] = evaluate(net512, sparse, args.eval, seed=888888)
+    res["eval_sparse_view"] = evaluate(net512, sparse, args.eval, seed=888888, budgets=budgets,
+                                       max_iters=args.max_iters, abs_targets=abs_t)
     log(json.dumps(res["eval_sparse_view"]))
     if args.out:
         with open(args.out, "w") as f:

@@ -81,3 +81,28 @@ def test_autotuner_picks_a_valid_shape_and_caches_it(gpu, tmp_path):
                              fp_split=c["fp_split"], bp_split=c["bp_split"], grid_blocks=c["grid_blocks"])
     ref = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(64 * 64, np.float32), b, 20)
     assert rel_l2(x.cpu().numpy(), ref) < 1e-5
+
+
+def test_sirt_plan_graph_replay(gpu):
+    # two problems captured once in a CUDA graph; replays after refilling the
+    # sinograms in place give the same images as direct batched solves
+    specs = [(64, 40, 0), (32, 24, 1)]
+    probs, sinos = [], []
+    for size, a, seed in specs:
+        g, b = _make(size, a, seed)
+        p = rt.Problem(_dev(g.angles), g.rhozero, g.deltarho, g.numrhos, size, _dev(b), 25, residuals=True)
+        probs.append(p)
+        sinos.append((g, b))
+    plan = rt.SirtPlan(probs)
+    for rep in range(2):
+        for p, (g, b) in zip(probs, sinos):
+            p.projections.copy_(_dev(b * (1.0 + 0.5 * rep)))
+        plan.launch()
+        outs = [p.out.clone() for p in probs]
+        direct = [rt.Problem(p.angles, p.rhozero, p.deltarho, p.numrhos, p.size, p.projections.clone(), 25)
+                  for p in probs]
+        rt.sirt_batch(direct)
+        for o, d in zip(outs, direct):
+            assert torch.equal(o, d.out)
+        for p in probs:
+            assert int(p.done[0].item()) == 25

@@ -30,5 +30,5 @@ def test_trained_warm_start_beats_plain_sirt(gpu):
     # the start is better than one plain update, and the gain is largest where
     # plain SIRT's own budget is short
     assert ev["warm_start_residual_mean"] < ev["plain_residual_after_1"]
-    k10 = ev["budgets"][0]
+    k10 = ev["rows"][0]
     assert k10["warm_iterations_mean"] < 0.7 * k10["plain_iterations_mean"], ev
