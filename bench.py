@@ -631,7 +631,7 @@ def main():
                        "step": "forward projection + backprojection", "l2": "flushed (512 MB write) before every step",
                        "parallelism": f"replicas x{world}"},
             "fp_ms": res["fp_ms"], "bp_ms": res["bp_ms"],
-            "gpu_launches": 8 * args.steps,
+            "gpu_launches": 9 * args.steps,
             "clocks": res["clocks"], "roofline": roofline}
     e = res["e2e"]
     if e is not None:

@@ -246,9 +246,11 @@ int synk_conv3x3_bf16(synk_context *ctx, const uint16_t *x, int32_t ldx, int32_t
                       int32_t H, int32_t W, const uint16_t *w, const float *bias, uint16_t *y, int32_t ldy,
                       int32_t yoff, int32_t Cout, int32_t epi, const uint16_t *mask, int32_t ldm, int32_t moff);
 
-/* dw[o][tap*Cin + i] += sum_p dy[p][o] * x[p + tap][i] from channel-major
- * dyT [Cout][B][H][W] and the three W-shifted channel-major copies
- * xT3 [3][Cin][B][H][W]; dw FP32 [Cout][9*Cin]. */
+/* dw[o][tap*Cin + i] += sum_p dy[p][o] * x[p + tap][i] from blocked copies
+ * with pixel chunks of c = 64 (W >= 64) or 32 pixels of one image row:
+ * dyT [B][H][W/c][Cout][c] and the three W-shifted copies
+ * xT3 [3][B][H][W/c][Cin][c] (copy k holds x[w + k - 1], zero outside the
+ * row); dw FP32 [Cout][9*Cin]. */
 int synk_conv3x3_wgrad_bf16(synk_context *ctx, const uint16_t *dyT, const uint16_t *xT3, float *dw, int32_t Cin,
                             int32_t Cout, int32_t B, int32_t H, int32_t W, int32_t ksplit);
 

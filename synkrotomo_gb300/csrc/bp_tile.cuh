@@ -56,7 +56,10 @@ __device__ __forceinline__ void bp_stage(const ProbGeom &P, int k0, BpStage &st)
 // from the centre (the second is never negative), so
 //   w0 = sat(h/b - |e - sqrt(2)/2| / b),  w1 = sat(c1 - e/b),  c1 = h/b - (1 - sqrt(2)/2)/b.
 // INRANGE: the host proved that every window [s0, s0+1] lies in [0, D).
-template <int PIX, bool UNIT, bool INRANGE>
+// SCALED: the sinogram rows of the staged (non-near-axis) angles are already
+// multiplied by their lbase (row_scale), which saves one multiply per
+// (pixel, angle); near-axis rows stay unscaled for bp_exact_angles.
+template <int PIX, bool UNIT, bool INRANGE, bool SCALED>
 __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, int kc, int kend, int kphase,
                                          int kstride, const float *__restrict__ sino, float xc, float yc0,
                                          float ystep, float (&acc)[PIX]) {
@@ -88,7 +91,8 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
                     v0 = ((unsigned)s0 < uD) ? __ldg(row + s0) : 0.0f;
                     v1 = ((unsigned)(s0 + 1) < uD) ? __ldg(row + s0 + 1) : 0.0f;
                 }
-                acc[m] = fmaf(le.x, fmaf(w1, v1, w0 * v0), acc[m]);
+                if constexpr (SCALED) acc[m] = fmaf(w1, v1, fmaf(w0, v0, acc[m]));
+                else acc[m] = fmaf(le.x, fmaf(w1, v1, w0 * v0), acc[m]);
             }
         } else {
             float t = fmaf(-yc0, g.y, -P.rhozero);
@@ -105,10 +109,16 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
                     const float w = __saturatef(fmaf(-fabsf(d), g.w, g.z));
                     if ((unsigned)det < uD) a = fmaf(w, __ldg(row + det), a);
                 }
-                acc[m] = fmaf(le.x, a, acc[m]);
+                acc[m] = SCALED ? acc[m] + a : fmaf(le.x, a, acc[m]);
             }
         }
     }
+}
+
+// Factor of sinogram row k in a SCALED backprojection: lbase, or 1 for a
+// near-axis angle (summed from the unscaled row by bp_exact_angles).
+__device__ __forceinline__ float row_scale(const AngleGeom *__restrict__ geom, int k) {
+    return __ldg(&geom[k].exact) ? 1.0f : __ldg(&geom[k].lbase);
 }
 
 // True when every pixel's two candidate detectors of the UNIT path lie in

@@ -206,7 +206,9 @@ int backward(synk_context *ctx, float *out, const float *angles, int64_t a, floa
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size_in, geom);
     AngleLists L;
     SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
-    SYNK_CUDA(launch_bp(P, L, projections, out, st), "backprojection kernel");
+    float *scaled;
+    SYNK_CUDA(sc.get(&scaled, (size_t)p), "cudaMallocAsync(scaled rows)");
+    SYNK_CUDA(launch_bp(P, L, projections, out, st, scaled), "backprojection kernel");
     return SYNK_OK;
 }
 
@@ -970,6 +972,6 @@ extern "C" int synk_backprojection_noalloc(synk_context *ctx, float *out, const 
     L.order = sc->order;
     L.exact = sc->exact;
     L.counts = sc->counts;
-    SYNK_CUDA(launch_bp(P, L, projections, out, st), "backprojection kernel");
+    SYNK_CUDA(launch_bp(P, L, projections, out, st, nullptr), "backprojection kernel");
     return SYNK_OK;
 }

@@ -95,11 +95,11 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
 }
 
 // Ray of a near-axis angle k, the reference's own expressions
-// (forwardprojection.fut:31-56), computed by the 32 lanes of a warp: lane l
-// takes rows l, l+32, ...; the lane sums are combined in a fixed order.
-// Returns the ray sum in every lane.
+// (forwardprojection.fut:31-56), computed by the 32 lanes of a warp over the
+// frame rows [jb, je): lane l takes rows jb+l, jb+l+32, ...; the lane sums are
+// combined in a fixed order.  Returns the sum in every lane.
 __device__ __forceinline__ float fp_exact_ray_warp(const ProbGeom &P, int k, int r, const float *__restrict__ xpad,
-                                                   const float *__restrict__ xTpad) {
+                                                   const float *__restrict__ xTpad, int jb = 0, int je = 1 << 30) {
     const int lane = threadIdx.x & 31;
     const AngleGeom g = load_geom(P.geom, k);
     const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));
@@ -107,7 +107,8 @@ __device__ __forceinline__ float fp_exact_ray_warp(const ProbGeom &P, int k, int
     const float intercept = __fdiv_rn(rho, g.cost);
     const float *img = (g.flat ? xTpad : xpad) + 1;
     float acc = 0.0f;
-    for (int i = -P.half + lane; i < P.half; i += 32)
+    const int iend = min(P.half, -P.half + je);
+    for (int i = -P.half + jb + lane; i < iend; i += 32)
         acc = __fadd_rn(acc, fp_row_exact<false>(img, P.N + 2, P.half, g.slope, intercept, g.lbase, i));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));

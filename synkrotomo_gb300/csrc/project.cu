@@ -162,48 +162,108 @@ cudaError_t launch_unpad(const float *xpad, float *x, int N, int nslices, cudaSt
 
 // ---- forward projection ---------------------------------------------------------
 
+// A block = 8 warps = 8/S detectors x S row parts (S = 1, 2, 4, 8): with few
+// angles (sparse-view data) the rays are split over rows so that enough warps
+// are in flight; the S partial sums of a ray are added in a fixed order.
+template <int S>
 __global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
                                                       const float *__restrict__ xTpad, float *__restrict__ sino) {
+    __shared__ float red[8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int grp = blockIdx.y;
     const int nsteep = __ldg(L.counts), nflat = __ldg(L.counts + 1);
     if (grp >= nsteep + nflat) return;              // block-uniform
-    const int r = blockIdx.x * 8 + warp;
-    if (r >= P.D) return;                           // warp-uniform
+    const int part = warp % S;
+    const int r = blockIdx.x * (8 / S) + warp / S;
+    const int rr = r < P.D ? r : P.D - 1;          // keep every warp for the block reduction
     const int k = __ldg(L.order + grp * 32 + lane);
-    const float v = fp_lane_ray(P, k, r, grp < nsteep ? xpad : xTpad, 0, P.N);
-    if (k >= 0) sino[(size_t)k * P.D + r] = v;
+    const int jb = part * P.N / S, je = (part + 1) * P.N / S;
+    float v = fp_lane_ray(P, r < P.D ? k : -1, rr, grp < nsteep ? xpad : xTpad, jb, je);
+    if (S > 1) {
+        red[warp][lane] = v;
+        __syncthreads();
+        if (part != 0) return;
+        for (int t = 1; t < S; ++t) v += red[warp + t][lane];
+    }
+    if (k >= 0 && r < P.D) sino[(size_t)k * P.D + r] = v;
 }
 
-// one warp per near-axis ray
+// near-axis rays: a warp per (ray, row part), 8/S rays per block
+template <int S>
 __global__ void __launch_bounds__(256) fp_exact_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
                                                        const float *__restrict__ xTpad, float *__restrict__ sino) {
+    __shared__ float red[8];
     const int nexact = __ldg(L.counts + 2);
-    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (r >= P.D) return;                           // warp-uniform
-    for (int e = blockIdx.y; e < nexact; e += gridDim.y) {
+    const int warp = threadIdx.x >> 5, part = warp % S;
+    const int r = blockIdx.x * (8 / S) + warp / S;
+    const int jb = part * P.N / S, je = (part + 1) * P.N / S;
+    for (int e = blockIdx.y; e < nexact; e += gridDim.y) {      // block-uniform
         const int k = __ldg(L.exact + e);
-        const float v = fp_exact_ray_warp(P, k, r, xpad, xTpad);
-        if ((threadIdx.x & 31) == 0) sino[(size_t)k * P.D + r] = v;
+        float v = r < P.D ? fp_exact_ray_warp(P, k, r, xpad, xTpad, jb, je) : 0.0f;
+        if (S > 1) {
+            __syncthreads();
+            if ((threadIdx.x & 31) == 0) red[warp] = v;
+            __syncthreads();
+            if (part == 0)
+                for (int t = 1; t < S; ++t) v = __fadd_rn(v, red[warp + t]);
+        }
+        if (part == 0 && r < P.D && (threadIdx.x & 31) == 0) sino[(size_t)k * P.D + r] = v;
     }
+}
+
+// Rows split S ways when the rays alone give too few warps to fill the GPU.
+static int fp_row_split(long long warps) {
+    int sms = 152, dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = (long long)sms * 48;
+    int S = 1;
+    while (S < 8 && warps * S < want) S *= 2;
+    return S;
 }
 
 cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad, const float *xTpad, float *sino,
                       cudaStream_t stream) {
-    dim3 grid((P.D + 7) / 8, (P.a + 31) / 32 + 2);
-    fp_lane_kernel<<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino);
+    // groups of 32 angles: at most ceil(a/32) + 2 (the steep/flat split adds one partial group each)
+    const int gmax = (P.a + 31) / 32 + 2;
+    const int S = fp_row_split((long long)((P.a + 31) / 32) * P.D);
+    const dim3 grid((P.D + 8 / S - 1) / (8 / S), gmax);
+    switch (S) {
+        case 1: fp_lane_kernel<1><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        case 2: fp_lane_kernel<2><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        case 4: fp_lane_kernel<4><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        default: fp_lane_kernel<8><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    dim3 ge((P.D + 7) / 8, 8);
-    fp_exact_kernel<<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino);
+    // near-axis angles: at most 4 in [0, 2 pi); rays x 8 angle slots must fill the GPU
+    const int SE = fp_row_split((long long)P.D * 2);
+    const dim3 ge((P.D + 8 / SE - 1) / (8 / SE), 8);
+    switch (SE) {
+        case 1: fp_exact_kernel<1><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        case 2: fp_exact_kernel<2><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        case 4: fp_exact_kernel<4><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        default: fp_exact_kernel<8><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+    }
     return cudaGetLastError();
 }
 
 // ---- backprojection ---------------------------------------------------------------
 
-template <bool UNIT, bool INRANGE>
-__global__ void __launch_bounds__(256) bp_tile_kernel(ProbGeom P, AngleLists L, const float *__restrict__ sino,
-                                                      float *__restrict__ out) {
+// sino_s[k][r] = sino[k][r] * row_scale(k): the rows of a SCALED backprojection.
+__global__ void __launch_bounds__(256) row_scale_kernel(ProbGeom P, const float *__restrict__ sino,
+                                                        float *__restrict__ sino_s) {
+    const int r = blockIdx.x * 256 + threadIdx.x;
+    const int k = blockIdx.y;
+    if (r >= P.D) return;
+    const size_t i = (size_t)k * P.D + r;
+    sino_s[i] = sino[i] * row_scale(P.geom, k);
+}
+
+// sino_s: the fast-path rows (scaled when SCALED, else sino itself); sino:
+// the unscaled rows read by the near-axis angles.
+template <bool UNIT, bool INRANGE, bool SCALED>
+__global__ void __launch_bounds__(256, 6) bp_tile_kernel(ProbGeom P, AngleLists L, const float *__restrict__ sino_s,
+                                                      const float *__restrict__ sino, float *__restrict__ out) {
     __shared__ BpStage st;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int col = blockIdx.x * 32 + lane;
@@ -216,7 +276,7 @@ __global__ void __launch_bounds__(256) bp_tile_kernel(ProbGeom P, AngleLists L, 
         bp_stage(P, kc, st);
         __syncthreads();
         float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        bp_chunk<4, UNIT, INRANGE>(P, st, kc, P.a, 0, 1, sino, xc, yc0, 8.0f, part);
+        bp_chunk<4, UNIT, INRANGE, SCALED>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
 #pragma unroll
         for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], part[m]);
     }
@@ -229,11 +289,21 @@ __global__ void __launch_bounds__(256) bp_tile_kernel(ProbGeom P, AngleLists L, 
     }
 }
 
-cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream) {
+cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
+                      float *scaled) {
     dim3 grid((P.N + 31) / 32, (P.N + 31) / 32);
-    if (bp_windows_in_range(P)) bp_tile_kernel<true, true><<<grid, 256, 0, stream>>>(P, L, sino, img);
-    else if (P.deltarho == 1.0f) bp_tile_kernel<true, false><<<grid, 256, 0, stream>>>(P, L, sino, img);
-    else bp_tile_kernel<false, false><<<grid, 256, 0, stream>>>(P, L, sino, img);
+    if (scaled) {
+        row_scale_kernel<<<dim3((P.D + 255) / 256, P.a), 256, 0, stream>>>(P, sino, scaled);
+        if (bp_windows_in_range(P)) bp_tile_kernel<true, true, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+        else if (P.deltarho == 1.0f)
+            bp_tile_kernel<true, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+        else bp_tile_kernel<false, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+    } else {
+        if (bp_windows_in_range(P)) bp_tile_kernel<true, true, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
+        else if (P.deltarho == 1.0f)
+            bp_tile_kernel<true, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
+        else bp_tile_kernel<false, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
+    }
     return cudaGetLastError();
 }
 

@@ -140,12 +140,13 @@ __device__ __forceinline__ int find_problem(const SirtParams &p, long long item,
     return lo;
 }
 
-// residual of one ray: e = b - fp; rr = R*e (SIRT.fut:33-36); returns e^2
+// residual of one ray: e = b - fp; rr = R*e (SIRT.fut:33-36), stored times the
+// row's lbase for the SCALED backprojection; returns e^2
 __device__ __forceinline__ double residual(const SirtProblem &q, int s, int k, int r, float fpv) {
     const size_t pr = (size_t)q.P.a * q.P.D;
     const size_t ray = (size_t)k * q.P.D + r;
     const float e = __fsub_rn(q.b[(size_t)s * pr + ray], fpv);
-    q.rr[(size_t)s * pr + ray] = __fmul_rn(q.R[ray], e);
+    q.rr[(size_t)s * pr + ray] = __fmul_rn(__fmul_rn(q.R[ray], e), row_scale(q.P.geom, k));
     return (double)e * (double)e;
 }
 
@@ -250,9 +251,9 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
             bp_stage(P, kc, sh.st);
             __syncthreads();
             float prt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            if (inrange) bp_chunk<4, true, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
-            else if (unit) bp_chunk<4, true, false>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
-            else bp_chunk<4, false, false>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            if (inrange) bp_chunk<4, true, true, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            else if (unit) bp_chunk<4, true, false, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            else bp_chunk<4, false, false, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
 #pragma unroll
             for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], prt[m]);
         }

@@ -303,7 +303,10 @@ struct AngleLists;
 cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStream_t stream);
 cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad, const float *xTpad, float *sino,
                       cudaStream_t stream);
-cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream);
+// scaled: scratch of a*D floats for the lbase-scaled rows (faster inner loop),
+// or null for the unscaled kernel (no scratch)
+cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
+                      float *scaled);
 cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, cudaStream_t stream);
 
 // compare.cu: the validation programs (diff, mse, sanityCheck) in one pass.

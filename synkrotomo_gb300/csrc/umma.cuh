@@ -42,19 +42,46 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Time limits of the spin waits are counted in SM clock cycles (clock64, a
+// register read) rather than %globaltimer, whose read is slow enough to
+// delay every hand-off between the pipeline's warps.  2.2 cycles per ns is
+// above the maximum SM clock, so a limit of limit_ns lasts at least limit_ns.
+__device__ __forceinline__ long long limit_cycles(unsigned long long limit_ns) {
+    return (long long)(limit_ns * 11ull / 5ull);
+}
+
 // Waits for the phase of `parity`; false when the limit ran out or another
 // thread of the kernel already failed (err != 0).  On timeout err is set.
+// The error word (a global load) is only polled once a wait has lasted about
+// 100 us, so healthy hand-offs never touch it.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, unsigned long long limit_ns) {
-    const unsigned long long t0 = now_ns();
-    for (uint32_t i = 0;; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long c0 = clock64();
+    const long long lim = limit_cycles(limit_ns);
+    for (uint32_t i = 1;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 63u) == 63u) {
-            if (*(volatile int *)err) return false;
-            if (now_ns() - t0 > limit_ns || i > (1u << 28)) {
+        if ((i & 1023u) == 0u) {
+            const long long dc = clock64() - c0;
+            if (dc > 220000ll && *(volatile int *)err) return false;
+            if (dc > lim || i > (1u << 30)) {
                 atomicExch(err, 3);   // SYNK_ETIMEOUT
                 return false;
             }
         }
+    }
+}
+
+// Wind-down wait for work this thread itself started (copies or MMAs in
+// flight): ignores other threads' failures, gives up after limit_ns.
+__device__ __forceinline__ bool mbar_drain(uint64_t *bar, uint32_t parity, unsigned long long limit_ns) {
+    const long long c0 = clock64();
+    const long long lim = limit_cycles(limit_ns);
+    for (uint32_t i = 0;; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 1023u) == 1023u && (clock64() - c0 > lim || i > (1u << 30))) return false;
     }
 }
 
@@ -72,6 +99,14 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, u
         "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6}], "
         "[%2];" ::"r"(smem_u32(dst)),
         "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2,
+                                            int c3, int c4) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6, "
+        "%7}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
         : "memory");
 }
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap *map) {
@@ -111,6 +146,11 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t row_bytes
     d |= swz << 61;
     return d;
 }
+// The same for a 128-byte-swizzled operand whose first row is not at a
+// 1024-byte pattern boundary (a view starting r rows into a TMA-written
+// tile).  The XOR pattern is taken from the absolute shared-memory address,
+// as TMA writes it, so the view needs no base offset.
+__device__ __forceinline__ uint64_t smem_desc_sw128_at(uint32_t saddr) { return smem_desc(saddr, 128u); }
 // Instruction descriptor of tcgen05.mma kind::f16: D = F32 (bits 4-5 = 1),
 // A = B = BF16 (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0),
 // N >> 3 in bits 17-22, M >> 4 in bits 24-28.

@@ -13,15 +13,17 @@
 // Operand modes (how the producer addresses A and B):
 //   MODE_GEMM   plain 2-D tensors (validation of the engine)
 //   MODE_CONV   implicit-GEMM 3x3 convolution, pad 1, NHWC BF16: K = 9 taps x
-//               input channels in chunks of 32; the A box of a tap is the
+//               input channels in chunks of 64 (128-byte rows, 128-byte
+//               swizzle) when Cin allows, else 32; the A box of a tap is the
 //               tile's 128 pixels shifted by the tap, read from a 4-D map
 //               (C, W, H, batch) whose out-of-bounds zeros are the padding.
 //               The backward-data pass is the same convolution of the output
 //               gradient with the tap-flipped, transposed weights.
-//   MODE_WGRAD  weight gradient: K = pixels (64 per chunk) of channel-major
-//               copies, A = dY^T (output channels), B = X^T shifted by the tap
-//               (three copies pre-shifted along W; the H shift is the TMA
-//               coordinate), split over K across CTAs with FP32 atomics.
+//   MODE_WGRAD  weight gradient: K = pixels, 64 (or 32) per chunk, of blocked
+//               copies [image][row][pixel chunk][channel][pixel]; A = dY
+//               (output channels), B = X shifted by the tap (three copies
+//               pre-shifted along W; the H shift is the TMA coordinate), split
+//               over K across CTAs with FP32 atomics.
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
@@ -39,190 +41,304 @@ __device__ __forceinline__ uint16_t f2bf(float x) {
 }
 __device__ __forceinline__ float bf2f(uint16_t x) { return __bfloat162float(__ushort_as_bfloat16(x)); }
 
+// The coordinates of one output tile (linear index t over gx x gy x gz).
+struct TileInfo {
+    int m0, n0, kbeg, nk, b, h0, w0, ky, kx, tap;
+};
+
+template <int MODE>
+__device__ __forceinline__ TileInfo tile_info(const GemmParams &p, long long t) {
+    TileInfo ti = {};
+    const int tx = (int)(t % p.gx);
+    const long long r1 = t / p.gx;
+    const int ty = (int)(r1 % p.gy);
+    const int tz = (int)(r1 / p.gy);
+    ti.n0 = ty * p.N;
+    ti.nk = p.nk;
+    if (MODE == MODE_GEMM) {
+        ti.m0 = tx * 128;
+    } else if (MODE == MODE_CONV || MODE == MODE_HALO) {
+        const int tiles_w = p.W / p.bw, tpi = tiles_w * (p.H / p.bh);
+        ti.b = tx / tpi;
+        const int r = tx - ti.b * tpi;
+        ti.h0 = (r / tiles_w) * p.bh;
+        ti.w0 = (r - (r / tiles_w) * tiles_w) * p.bw;
+    } else {   // MODE_WGRAD
+        // taps vary fastest: the CTAs running at one time cover the nine taps of
+        // the same pixel range, which then come from L2 instead of HBM
+        ti.m0 = tx * 128;
+        const int ks = tz / 9;
+        ti.tap = tz - ks * 9;
+        ti.ky = ti.tap / 3;
+        ti.kx = ti.tap - ti.ky * 3;
+        const long long nbk = (long long)p.Bn * p.nb_h * p.nb_w;
+        ti.kbeg = (int)(nbk * ks / p.ksplit);
+        ti.nk = (int)(nbk * (ks + 1) / p.ksplit) - ti.kbeg;
+    }
+    return ti;
+}
+
+// Persistent: one CTA per SM walks tiles t = blockIdx.x, += gridDim.x.  The
+// shared-memory stage ring runs continuously across tiles, and the FP32
+// accumulator is double-buffered in TMEM (2 x ncols columns): the MMA warp
+// fills buffer (i & 1) for tile i while the epilogue warps drain the other.
+//   full[s]   TMA -> MMA     (expect_tx bytes)       empty[s]  MMA -> TMA (tcgen05.commit)
+//   tfull[j]  MMA -> epilogue (tcgen05.commit)       tempty[j] epilogue -> MMA (4 warp arrivals)
 template <int MODE, int EPI>
 __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CUtensorMap tmA,
                                                       const __grid_constant__ CUtensorMap tmB, const GemmParams p) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     uint8_t *smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    const uint32_t aBytes = 128u * (uint32_t)p.kbytes;
-    const uint32_t bBytes = (((uint32_t)p.N * (uint32_t)p.kbytes + 1023u) / 1024u) * 1024u;
+    // MODE_HALO: A = one 130-pixel row strip (128-byte rows), B = the 3 taps kx of the strip's ky
+    const uint32_t aBytes = MODE == MODE_HALO ? p.aStage : 128u * (uint32_t)p.kbytes;
+    const uint32_t bTap = (((uint32_t)p.N * (uint32_t)(MODE == MODE_HALO ? 128 : p.kbytes) + 1023u) / 1024u) * 1024u;
+    const uint32_t bBytes = MODE == MODE_HALO ? 3u * bTap : bTap;
     const uint32_t stageBytes = aBytes + bBytes;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)p.stages * stageBytes);
-    uint64_t *empty = full + p.stages;
-    uint64_t *accum = empty + p.stages;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
+    const int S = p.stages;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stageBytes);
+    uint64_t *empty = full + S;
+    uint64_t *tfull = empty + S;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *drain = tempty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    float *sbias = reinterpret_cast<float *>(tmem_slot + 4);    // [gy * N] epilogue bias
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
-        tmem_alloc(tmem_slot, (uint32_t)p.ncols);
+        tmem_alloc(tmem_slot, 2u * (uint32_t)p.ncols);
         tmem_relinquish();
     }
     if (warp == 1 && lane == 0) {
-        for (int s = 0; s < p.stages; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accum, 1);
+        for (int j = 0; j < 2; ++j) {
+            mbar_init(&tfull[j], 1);
+            mbar_init(&tempty[j], 4);
+        }
+        mbar_init(drain, 1);
         fence_mbar_init();
     }
     if (warp == 0 && lane == 0) {
         tma_prefetch_desc(&tmA);
         tma_prefetch_desc(&tmB);
     }
+    if (EPI == EPI_BIAS_RELU || EPI == EPI_BIAS)
+        for (int i = threadIdx.x; i < p.gy * p.N; i += blockDim.x) sbias[i] = p.bias[i];
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-
-    // ---- this CTA's tile and K range ----
-    int m0 = 0, n0 = blockIdx.y * p.N, kbeg = 0, nk = p.nk;
-    int b = 0, h0 = 0, w0 = 0, ky = 0, kx = 0;
-    if (MODE == MODE_GEMM) {
-        m0 = blockIdx.x * 128;
-    } else if (MODE == MODE_CONV) {
-        const int tiles_w = p.W / p.bw, tpi = tiles_w * (p.H / p.bh);
-        const int mt = blockIdx.x;
-        b = mt / tpi;
-        const int r = mt - b * tpi;
-        h0 = (r / tiles_w) * p.bh;
-        w0 = (r - (r / tiles_w) * tiles_w) * p.bw;
-    } else {   // MODE_WGRAD
-        m0 = blockIdx.x * 128;
-        const int tap = blockIdx.z / p.ksplit, ks = blockIdx.z - tap * p.ksplit;
-        ky = tap / 3;
-        kx = tap - ky * 3;
-        const long long nbk = (long long)p.Bn * p.nb_h * p.nb_w;
-        kbeg = (int)(nbk * ks / p.ksplit);
-        nk = (int)(nbk * (ks + 1) / p.ksplit) - kbeg;
-    }
+    const long long ntiles = p.ntiles;
 
     if (warp == 0) {
         if (lane == 0) {
             // ---- TMA producer ----
-            int issued = 0;
-            for (int kc = 0; kc < nk; ++kc) {
-                const int s = kc % p.stages;
-                const uint32_t ph = (uint32_t)(kc / p.stages) & 1u;
-                if (kc >= p.stages && !mbar_wait(&empty[s], ph ^ 1u, p.err, p.limit_ns)) break;
-                uint8_t *As = smem + (size_t)s * stageBytes;
-                uint8_t *Bs = As + aBytes;
-                mbar_arrive_expect_tx(&full[s], p.bytesA + p.bytesB);
-                if (MODE == MODE_GEMM) {
-                    const int ke = p.kbytes / 2;
-                    tma_load_2d(As, &tmA, &full[s], kc * ke, m0);
-                    tma_load_2d(Bs, &tmB, &full[s], kc * ke, n0);
-                } else if (MODE == MODE_CONV) {
-                    const int tap = kc / p.cchunks, cc = kc - tap * p.cchunks;
-                    const int tky = tap / 3, tkx = tap - tky * 3;
-                    tma_load_4d(As, &tmA, &full[s], cc * 32, w0 + tkx - 1, h0 + tky - 1, b);
-                    tma_load_2d(Bs, &tmB, &full[s], tap * p.Cin + cc * 32, n0);
-                } else {
-                    const int pb = kbeg + kc;
-                    const int per_img = p.nb_h * p.nb_w;
-                    const int bb = pb / per_img;
-                    const int r = pb - bb * per_img;
-                    const int hb = r / p.nb_w, wb = r - (r / p.nb_w) * p.nb_w;
-                    tma_load_4d(As, &tmA, &full[s], wb * p.bwk, hb * p.bhk, bb, m0);
-                    tma_load_4d(Bs, &tmB, &full[s], wb * p.bwk, hb * p.bhk + ky - 1, bb, kx * p.Cin + n0);
+            long long g = 0;   // chunks issued by this CTA
+            bool fail = false;
+            for (long long t = blockIdx.x; t < ntiles && !fail; t += gridDim.x) {
+                const TileInfo ti = tile_info<MODE>(p, t);
+                for (int kc = 0; kc < ti.nk; ++kc) {
+                    const int s = (int)(g % S);
+                    const uint32_t ph = (uint32_t)(g / S) & 1u;
+                    if (g >= S && !mbar_wait(&empty[s], ph ^ 1u, p.err, p.limit_ns)) {
+                        fail = true;
+                        break;
+                    }
+                    uint8_t *As = smem + (size_t)s * stageBytes;
+                    uint8_t *Bs = As + aBytes;
+                    mbar_arrive_expect_tx(&full[s], p.bytesA + p.bytesB);
+                    if (MODE == MODE_GEMM) {
+                        const int ke = p.kbytes / 2;
+                        tma_load_2d(As, &tmA, &full[s], kc * ke, ti.m0);
+                        tma_load_2d(Bs, &tmB, &full[s], kc * ke, ti.n0);
+                    } else if (MODE == MODE_HALO) {
+                        // chunk = (ky, channel chunk cc): the strip of row h0+ky-1,
+                        // pixels w0-1 .. w0+128, and the weights of taps (ky, 0..2)
+                        // (64-channel boxes; channels >= Cin are out of bounds and read as 0)
+                        const int ky = kc / p.cchunks, cc = kc - ky * p.cchunks;
+                        tma_load_4d(As, &tmA, &full[s], cc * 64, ti.w0 - 1, ti.h0 + ky - 1, ti.b);
+#pragma unroll
+                        for (int kx = 0; kx < 3; ++kx)
+                            tma_load_2d(Bs + kx * bTap, &tmB, &full[s], (ky * 3 + kx) * p.Cin + cc * 64, ti.n0);
+                    } else if (MODE == MODE_CONV) {
+                        const int tap = kc / p.cchunks, cc = kc - tap * p.cchunks;
+                        const int tky = tap / 3, tkx = tap - tky * 3;
+                        const int cw = p.kbytes / 2;   // channels per chunk
+                        tma_load_4d(As, &tmA, &full[s], cc * cw, ti.w0 + tkx - 1, ti.h0 + tky - 1, ti.b);
+                        tma_load_2d(Bs, &tmB, &full[s], tap * p.Cin + cc * cw, ti.n0);
+                    } else {
+                        const int pb = ti.kbeg + kc;
+                        const int per_img = p.nb_h * p.nb_w;
+                        const int bb = pb / per_img;
+                        const int r = pb - bb * per_img;
+                        const int hb = r / p.nb_w, wb = r - (r / p.nb_w) * p.nb_w;
+                        // blocked operands [image][row][pixel chunk][channel][pixel]: a box is
+                        // one contiguous block; the tap's row shift is the H coordinate (zero
+                        // outside the image) and its column shift the pre-shifted copy kx
+                        tma_load_5d(As, &tmA, &full[s], 0, ti.m0, wb, hb, bb);
+                        tma_load_5d(Bs, &tmB, &full[s], 0, ti.n0, wb, hb + ti.ky - 1, ti.kx * p.Bn + bb);
+                    }
+                    ++g;
                 }
-                issued = kc + 1;
             }
-            // no copy may still be landing when the CTA exits: wait for the last
-            // use of every stage (immediate on the normal path)
-            const int first = issued > p.stages ? issued - p.stages : 0;
-            for (int kc = first; kc < issued; ++kc)
-                mbar_wait(&full[kc % p.stages], (uint32_t)(kc / p.stages) & 1u, p.err, p.limit_ns);
+            // no copy may still be landing when the CTA exits: wait (bounded) for
+            // the last use of every stage (immediate on the normal path)
+            const long long first = g > S ? g - S : 0;
+            for (long long c = first; c < g; ++c) mbar_drain(&full[c % S], (uint32_t)(c / S) & 1u, p.limit_ns);
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // ---- MMA issuer ----
             const uint32_t idesc = idesc_bf16(128, p.N);
             const uint32_t kbytes = (uint32_t)p.kbytes;
-            for (int kc = 0; kc < nk; ++kc) {
-                const int s = kc % p.stages;
-                const uint32_t ph = (uint32_t)(kc / p.stages) & 1u;
-                if (!mbar_wait(&full[s], ph, p.err, p.limit_ns)) break;
+            long long g = 0;
+            int li = 0;
+            bool fail = false;
+            for (long long t = blockIdx.x; t < ntiles && !fail; t += gridDim.x, ++li) {
+                const TileInfo ti = tile_info<MODE>(p, t);
+                const int ab = li & 1;
+                const uint32_t dt = tmem + (uint32_t)(ab * p.ncols);
+                if (li >= 2 && !mbar_wait(&tempty[ab], (uint32_t)((li >> 1) - 1) & 1u, p.err, p.limit_ns)) break;
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(smem + (size_t)s * stageBytes);
-                const uint32_t b0 = a0 + aBytes;
-                for (uint32_t kk = 0; kk < kbytes / 32u; ++kk) {
-                    mma_bf16(tmem, smem_desc(a0 + kk * 32u, kbytes), smem_desc(b0 + kk * 32u, kbytes), idesc,
-                             (kc | (int)kk) != 0 ? 1u : 0u);
+                for (int kc = 0; kc < ti.nk; ++kc, ++g) {
+                    const int s = (int)(g % S);
+                    const uint32_t ph = (uint32_t)(g / S) & 1u;
+                    if (!mbar_wait(&full[s], ph, p.err, p.limit_ns)) {
+                        fail = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(smem + (size_t)s * stageBytes);
+                    const uint32_t b0 = a0 + aBytes;
+                    if (MODE == MODE_HALO) {
+                        // tap kx reads the strip from row kx (pixel w0+kx-1); only the
+                        // chunk's valid channels (32 or 64) are multiplied
+                        const int cc = kc % p.cchunks;
+                        const uint32_t ksteps = (uint32_t)min(64, p.Cin - 64 * cc) / 16u;
+                        for (uint32_t kx = 0; kx < 3u; ++kx)
+                            for (uint32_t kk = 0; kk < ksteps; ++kk)
+                                mma_bf16(dt, smem_desc_sw128_at(a0 + kx * 128u + kk * 32u),
+                                         smem_desc(b0 + kx * bTap + kk * 32u, 128u), idesc,
+                                         (kc | (int)kx | (int)kk) != 0 ? 1u : 0u);
+                    } else {
+                        for (uint32_t kk = 0; kk < kbytes / 32u; ++kk) {
+                            mma_bf16(dt, smem_desc(a0 + kk * 32u, kbytes), smem_desc(b0 + kk * 32u, kbytes), idesc,
+                                     (kc | (int)kk) != 0 ? 1u : 0u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
                 }
-                mma_commit(&empty[s]);
+                if (!fail) mma_commit(&tfull[ab]);
             }
-            mma_commit(accum);     // also issued on an early exit: completes when issued MMAs have
+            // every issued MMA has completed before TMEM is freed
+            mma_commit(drain);
+            mbar_drain(drain, 0u, p.limit_ns);
         }
     } else {
-        // ---- epilogue (warps 2..5) ----
+        // ---- epilogue (warps 2..5): TMEM lanes 32*(warp % 4) .. +31 ----
         const int q = warp & 3;
         const int row = q * 32 + lane;
-        const bool ok = mbar_wait(accum, 0u, p.err, p.limit_ns) && nk > 0;
-        tc_fence_after();
-        // tcgen05.ld is warp-collective: decide once per warp
-        const bool good = __all_sync(0xffffffffu, ok && *(volatile int *)p.err == 0);
-        // output position of this row
-        long long pix = 0;
-        bool rvalid = true;
-        if (MODE == MODE_GEMM) {
-            rvalid = m0 + row < p.M;
-        } else if (MODE == MODE_CONV) {
-            const int h = h0 + row / p.bw, w = w0 + (row - (row / p.bw) * p.bw);
-            pix = ((long long)b * p.H + h) * p.W + w;
-        } else {
-            rvalid = m0 + row < p.mvalid;
-        }
-        for (int c0 = 0; c0 < p.N; c0 += 32) {
-            float v[32];
-            if (good) tmem_ld_32x32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-            if (!good || !rvalid) continue;
-            const int nbase = n0 + c0;
-            const int nval = min(32, p.N - c0);
-            if (EPI == EPI_F32) {
-                float *o = reinterpret_cast<float *>(p.out) + (long long)(m0 + row) * p.ldo + nbase;
-                for (int j = 0; j < nval; ++j) o[j] = v[j];
-            } else if (EPI == EPI_ATOMIC) {
-                const int tap = blockIdx.z / p.ksplit;
-                float *o = reinterpret_cast<float *>(p.out) + (long long)(m0 + row) * p.ldo + tap * p.Cin + nbase;
-                const int lim = min(nval, p.Cin - nbase);
-                for (int j = 0; j < lim; ++j) atomicAdd(o + j, v[j]);
+        int li = 0;
+        for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++li) {
+            const TileInfo ti = tile_info<MODE>(p, t);
+            const int ab = li & 1;
+            const bool ok = mbar_wait(&tfull[ab], (uint32_t)(li >> 1) & 1u, p.err, p.limit_ns);
+            tc_fence_after();
+            // tcgen05.ld is warp-collective: decide once per warp
+            const bool good = __all_sync(0xffffffffu, ok && *(volatile int *)p.err == 0);
+            if (!good) break;
+            // a split-K tile with no chunks contributes nothing (its buffer was not written)
+            const int ncol = ti.nk > 0 ? p.N : 0;
+            long long pix = 0;
+            bool rvalid = true;
+            if (MODE == MODE_GEMM) {
+                rvalid = ti.m0 + row < p.M;
+            } else if (MODE == MODE_CONV || MODE == MODE_HALO) {
+                const int h = ti.h0 + row / p.bw, w = ti.w0 + (row - (row / p.bw) * p.bw);
+                pix = ((long long)ti.b * p.H + h) * p.W + w;
             } else {
-                uint16_t *o = reinterpret_cast<uint16_t *>(p.out) + pix * p.ldo + p.coff + nbase;
-                uint32_t pk[16];
+                rvalid = ti.m0 + row < p.mvalid;
+            }
+            const uint32_t tbase = tmem + (uint32_t)(ab * p.ncols) + ((uint32_t)(q * 32) << 16);
+            for (int c0 = 0; c0 < ncol; c0 += 32) {
+                float v[32];
+                tmem_ld_32x32(tbase + (uint32_t)c0, v);
+                if (!rvalid) continue;
+                const int nbase = ti.n0 + c0;
+                const int nval = min(32, p.N - c0);
+                if (EPI == EPI_F32) {
+                    float *o = reinterpret_cast<float *>(p.out) + (long long)(ti.m0 + row) * p.ldo + nbase;
 #pragma unroll
-                for (int j = 0; j < 32; j += 2) {
-                    float x0 = v[j], x1 = v[j + 1];
-                    if (EPI == EPI_BIAS_RELU || EPI == EPI_BIAS) {
-                        x0 += p.bias[nbase + j];
-                        x1 += p.bias[nbase + j + 1];
-                        if (EPI == EPI_BIAS_RELU) {
-                            x0 = fmaxf(x0, 0.0f);
-                            x1 = fmaxf(x1, 0.0f);
-                        }
-                    } else if (EPI == EPI_MASK) {
-                        const uint16_t *mk = p.mask + pix * p.ldm + p.moff + nbase + j;
-                        x0 = bf2f(mk[0]) > 0.0f ? x0 : 0.0f;
-                        x1 = bf2f(mk[1]) > 0.0f ? x1 : 0.0f;
-                    }
-                    pk[j / 2] = (uint32_t)f2bf(x0) | ((uint32_t)f2bf(x1) << 16);
-                }
-                if (nval == 32) {
-                    uint4 *o4 = reinterpret_cast<uint4 *>(o);
+                    for (int j = 0; j < 32; ++j)
+                        if (j < nval) o[j] = v[j];
+                } else if (EPI == EPI_ATOMIC) {
+                    float *o = reinterpret_cast<float *>(p.out) + (long long)(ti.m0 + row) * p.ldo + ti.tap * p.Cin +
+                               nbase;
+                    const int lim = min(nval, p.Cin - nbase);
 #pragma unroll
-                    for (int t = 0; t < 4; ++t) o4[t] = make_uint4(pk[4 * t], pk[4 * t + 1], pk[4 * t + 2], pk[4 * t + 3]);
+                    for (int j = 0; j < 32; ++j)
+                        if (j < lim) atomicAdd(o + j, v[j]);
                 } else {
-                    uint32_t *o2 = reinterpret_cast<uint32_t *>(o);
-                    for (int t = 0; t < nval / 2; ++t) o2[t] = pk[t];
+                    uint16_t *o = reinterpret_cast<uint16_t *>(p.out) + pix * p.ldo + p.coff + nbase;
+                    uint32_t pk[16];
+                    uint32_t mw[16];
+                    if (EPI == EPI_MASK) {
+                        const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + pix * p.ldm + p.moff + nbase);
+#pragma unroll
+                        for (int t4 = 0; t4 < 4; ++t4) {
+                            const uint4 u = (t4 * 8 < nval) ? mk[t4] : make_uint4(0u, 0u, 0u, 0u);
+                            mw[4 * t4] = u.x;
+                            mw[4 * t4 + 1] = u.y;
+                            mw[4 * t4 + 2] = u.z;
+                            mw[4 * t4 + 3] = u.w;
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 32; j += 2) {
+                        float x0 = v[j], x1 = v[j + 1];
+                        if (EPI == EPI_BIAS_RELU || EPI == EPI_BIAS) {
+                            x0 += sbias[nbase + j];
+                            x1 += sbias[nbase + j + 1];
+                            if (EPI == EPI_BIAS_RELU) {
+                                x0 = fmaxf(x0, 0.0f);
+                                x1 = fmaxf(x1, 0.0f);
+                            }
+                        } else if (EPI == EPI_MASK) {
+                            // BF16 > 0: sign bit clear and not +0 (the bits of a positive value)
+                            const uint32_t m = mw[j / 2];
+                            const uint32_t m0 = m & 0xffffu, m1 = m >> 16;
+                            x0 = (m0 != 0u && m0 < 0x8000u && m0 <= 0x7f80u) ? x0 : 0.0f;
+                            x1 = (m1 != 0u && m1 < 0x8000u && m1 <= 0x7f80u) ? x1 : 0.0f;
+                        }
+                        pk[j / 2] = (uint32_t)f2bf(x0) | ((uint32_t)f2bf(x1) << 16);
+                    }
+                    if (nval == 32) {
+                        uint4 *o4 = reinterpret_cast<uint4 *>(o);
+#pragma unroll
+                        for (int tt = 0; tt < 4; ++tt)
+                            o4[tt] = make_uint4(pk[4 * tt], pk[4 * tt + 1], pk[4 * tt + 2], pk[4 * tt + 3]);
+                    } else {
+                        uint32_t *o2 = reinterpret_cast<uint32_t *>(o);
+#pragma unroll
+                        for (int tt = 0; tt < 16; ++tt)
+                            if (tt < nval / 2) o2[tt] = pk[tt];
+                    }
                 }
             }
+            // this warp's reads of the buffer are complete: the MMA warp may reuse it
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[ab]);
         }
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        tmem_dealloc(tmem, (uint32_t)p.ncols);
+        tmem_dealloc(tmem, 2u * (uint32_t)p.ncols);
     }
 }
 
@@ -265,24 +381,38 @@ static int pow2_cols(int n) {
     return c;
 }
 
-static size_t smem_bytes(const GemmParams &p) {
-    const size_t a = 128u * p.kbytes, b = ((size_t)p.N * p.kbytes + 1023) / 1024 * 1024;
-    return 1024 + (size_t)p.stages * (a + b) + 8 * (2 * p.stages + 1) + 16;
+static size_t stage_bytes(const GemmParams &p, bool halo) {
+    const size_t btap = ((size_t)p.N * (halo ? 128 : p.kbytes) + 1023) / 1024 * 1024;
+    return halo ? (size_t)p.aStage + 3 * btap : 128u * (size_t)p.kbytes + btap;
+}
+
+static size_t smem_bytes(const GemmParams &p, int gy, bool halo) {
+    return 1024 + (size_t)p.stages * stage_bytes(p, halo) + 8 * (2 * p.stages + 5) + 16 + 4 * (size_t)gy * p.N;
 }
 
 static int pick_stages(int N, int kbytes) {
     const size_t a = 128u * kbytes, b = ((size_t)N * kbytes + 1023) / 1024 * 1024;
     int s = (int)((200 * 1024) / (a + b));
-    return s > 8 ? 8 : (s < 2 ? 2 : s);
+    return s > 16 ? 16 : (s < 2 ? 2 : s);
 }
 
+// Persistent launch: min(tiles, SMs) CTAs (one per SM: ~200 KB of stages)
+// walk the gx x gy x gz tiles.
 template <int MODE, int EPI>
-static cudaError_t launch(const CUtensorMap &A, const CUtensorMap &B, const GemmParams &p, dim3 grid,
-                          cudaStream_t st) {
-    const size_t smem = smem_bytes(p);
+static cudaError_t launch(const CUtensorMap &A, const CUtensorMap &B, GemmParams p, dim3 tiles, cudaStream_t st) {
+    const size_t smem = smem_bytes(p, (int)tiles.y, MODE == MODE_HALO);
     cudaError_t e = cudaFuncSetAttribute(umma_kernel<MODE, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    p.gx = (int)tiles.x;
+    p.gy = (int)tiles.y;
+    p.gz = (int)tiles.z;
+    p.ntiles = (long long)tiles.x * tiles.y * tiles.z;
+    if (p.ntiles == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)(p.ntiles < sms ? p.ntiles : sms);
     umma_kernel<MODE, EPI><<<grid, 192, smem, st>>>(A, B, p);
     return cudaGetLastError();
 }
@@ -314,29 +444,31 @@ cudaError_t gemm_bf16(const uint16_t *A, const uint16_t *B, float *C, int M, int
     return launch<MODE_GEMM, EPI_F32>(ta, tb, p, dim3(M / 128, 1, 1), st);
 }
 
-cudaError_t conv3x3(const ConvArgs &c, int epi, int *err, unsigned long long limit_ns, cudaStream_t st) {
-    if (c.Cin % 32 || c.Cout % 16 || (c.ldx % 8) || (c.xoff % 8) || (c.ldy % 8) || (c.yoff % 8))
-        return cudaErrorInvalidValue;
-    // N tiles of at most 256 output channels (TMEM columns / UMMA N)
-    const int ntile = c.Cout <= 256 ? c.Cout : (c.Cout % 192 == 0 ? 192 : (c.Cout % 128 == 0 ? 128 : 0));
-    if (ntile == 0) return cudaErrorInvalidValue;
-    const int bw = c.W >= 128 ? 128 : c.W;
-    const int bh = 128 / bw;
-    if (128 % bw || c.W % bw || c.H % bh) return cudaErrorInvalidValue;
+// Image rows of 128k pixels: a tile is 128 pixels of one row, and per input
+// row ky and 64-channel chunk ONE strip of 130 pixels (halo of one on each
+// side) is loaded; the three taps kx are views of it shifted by kx rows.
+// Compared with a box per tap this moves a third of the input through TMA.
+static cudaError_t conv3x3_halo(const ConvArgs &c, int epi, int ntile, int *err, unsigned long long limit_ns,
+                                cudaStream_t st) {
     GemmParams p = {};
     p.N = ntile;
     p.ncols = pow2_cols(ntile);
-    p.kbytes = 64;
-    p.cchunks = c.Cin / 32;
-    p.nk = 9 * p.cchunks;
-    p.stages = pick_stages(ntile, 64);
+    p.kbytes = 128;
+    p.cchunks = (c.Cin + 63) / 64;
+    p.nk = 3 * p.cchunks;
+    p.aStage = (130u * 128u + 1023u) / 1024u * 1024u;
     p.H = c.H;
     p.W = c.W;
     p.Cin = c.Cin;
-    p.bw = bw;
-    p.bh = bh;
-    p.bytesA = 128u * 64u;
-    p.bytesB = (uint32_t)ntile * 64u;
+    p.bw = 128;
+    p.bh = 1;
+    p.bytesA = 130u * 128u;
+    p.bytesB = 3u * (uint32_t)ntile * 128u;
+    {
+        const size_t st1 = stage_bytes(p, true);
+        int s = (int)((200 * 1024) / st1);
+        p.stages = s > 16 ? 16 : (s < 2 ? 2 : s);
+    }
     p.out = c.y;
     p.ldo = c.ldy;
     p.coff = c.yoff;
@@ -349,12 +481,70 @@ cudaError_t conv3x3(const ConvArgs &c, int epi, int *err, unsigned long long lim
     CUtensorMap ta, tb;
     const uint64_t da[4] = {(uint64_t)c.Cin, (uint64_t)c.W, (uint64_t)c.H, (uint64_t)c.B};
     const uint64_t sa[3] = {(uint64_t)c.ldx * 2, (uint64_t)c.ldx * 2 * c.W, (uint64_t)c.ldx * 2 * c.W * c.H};
-    const uint32_t ba[4] = {32, (uint32_t)bw, (uint32_t)bh, 1};
+    const uint32_t ba[4] = {64, 130, 1, 1};
     const uint64_t db[2] = {(uint64_t)9 * c.Cin, (uint64_t)c.Cout}, sb[1] = {(uint64_t)9 * c.Cin * 2};
-    const uint32_t bbx[2] = {32, (uint32_t)ntile};
+    const uint32_t bbx[2] = {64, (uint32_t)ntile};
     cudaError_t e;
-    if ((e = tensor_map(&ta, c.x + c.xoff, 4, da, sa, ba, 64)) != cudaSuccess) return e;
-    if ((e = tensor_map(&tb, c.w, 2, db, sb, bbx, 64)) != cudaSuccess) return e;
+    if ((e = tensor_map(&ta, c.x + c.xoff, 4, da, sa, ba, 128)) != cudaSuccess) return e;
+    if ((e = tensor_map(&tb, c.w, 2, db, sb, bbx, 128)) != cudaSuccess) return e;
+    const dim3 grid((unsigned)((long long)c.B * c.H * c.W / 128), (unsigned)(c.Cout / ntile), 1);
+    switch (epi) {
+        case EPI_BIAS_RELU: return launch<MODE_HALO, EPI_BIAS_RELU>(ta, tb, p, grid, st);
+        case EPI_BIAS: return launch<MODE_HALO, EPI_BIAS>(ta, tb, p, grid, st);
+        case EPI_MASK: return launch<MODE_HALO, EPI_MASK>(ta, tb, p, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t conv3x3(const ConvArgs &c, int epi, int *err, unsigned long long limit_ns, cudaStream_t st) {
+    if (c.Cin % 32 || c.Cout % 16 || (c.ldx % 8) || (c.xoff % 8) || (c.ldy % 8) || (c.yoff % 8))
+        return cudaErrorInvalidValue;
+    if (epi == EPI_MASK && (!c.mask || (c.ldm % 8) || (c.moff % 8))) return cudaErrorInvalidValue;
+    // N tiles of at most 256 output channels (TMEM columns / UMMA N)
+    const int ntile = c.Cout <= 256 ? c.Cout : (c.Cout % 192 == 0 ? 192 : (c.Cout % 128 == 0 ? 128 : 0));
+    if (ntile == 0) return cudaErrorInvalidValue;
+    // the row-strip form when a tile is one image row and two stages fit
+    if (c.W % 128 == 0 && 17408 + 3 * ((ntile * 128 + 1023) / 1024 * 1024) <= 100 * 1024)
+        return conv3x3_halo(c, epi, ntile, err, limit_ns, st);
+    const int bw = c.W >= 128 ? 128 : c.W;
+    const int bh = 128 / bw;
+    if (128 % bw || c.W % bw || c.H % bh) return cudaErrorInvalidValue;
+    // K chunks of 64 channels (128-byte rows, 128-byte swizzle) where Cin allows,
+    // else 32 (64-byte rows): TMA moves long rows at a higher rate
+    const int cw = c.Cin % 64 == 0 ? 64 : 32;
+    const int kb = 2 * cw;
+    GemmParams p = {};
+    p.N = ntile;
+    p.ncols = pow2_cols(ntile);
+    p.kbytes = kb;
+    p.cchunks = c.Cin / cw;
+    p.nk = 9 * p.cchunks;
+    p.stages = pick_stages(ntile, kb);
+    p.H = c.H;
+    p.W = c.W;
+    p.Cin = c.Cin;
+    p.bw = bw;
+    p.bh = bh;
+    p.bytesA = 128u * (uint32_t)kb;
+    p.bytesB = (uint32_t)ntile * (uint32_t)kb;
+    p.out = c.y;
+    p.ldo = c.ldy;
+    p.coff = c.yoff;
+    p.bias = c.bias;
+    p.mask = c.mask;
+    p.ldm = c.ldm;
+    p.moff = c.moff;
+    p.err = err;
+    p.limit_ns = limit_ns;
+    CUtensorMap ta, tb;
+    const uint64_t da[4] = {(uint64_t)c.Cin, (uint64_t)c.W, (uint64_t)c.H, (uint64_t)c.B};
+    const uint64_t sa[3] = {(uint64_t)c.ldx * 2, (uint64_t)c.ldx * 2 * c.W, (uint64_t)c.ldx * 2 * c.W * c.H};
+    const uint32_t ba[4] = {(uint32_t)cw, (uint32_t)bw, (uint32_t)bh, 1};
+    const uint64_t db[2] = {(uint64_t)9 * c.Cin, (uint64_t)c.Cout}, sb[1] = {(uint64_t)9 * c.Cin * 2};
+    const uint32_t bbx[2] = {(uint32_t)cw, (uint32_t)ntile};
+    cudaError_t e;
+    if ((e = tensor_map(&ta, c.x + c.xoff, 4, da, sa, ba, kb)) != cudaSuccess) return e;
+    if ((e = tensor_map(&tb, c.w, 2, db, sb, bbx, kb)) != cudaSuccess) return e;
     const dim3 grid((unsigned)((long long)c.B * c.H * c.W / 128), (unsigned)(c.Cout / ntile), 1);
     switch (epi) {
         case EPI_BIAS_RELU: return launch<MODE_CONV, EPI_BIAS_RELU>(ta, tb, p, grid, st);
@@ -396,15 +586,18 @@ cudaError_t conv3x3_wgrad(const WgradArgs &w, int *err, unsigned long long limit
     p.err = err;
     p.limit_ns = limit_ns;
     CUtensorMap ta, tb;
-    const uint64_t pix = (uint64_t)w.B * w.H * w.W;
-    const uint64_t da[4] = {(uint64_t)w.W, (uint64_t)w.H, (uint64_t)w.B, (uint64_t)w.Cout};
-    const uint64_t sa[3] = {(uint64_t)w.W * 2, (uint64_t)w.W * w.H * 2, pix * 2};
-    const uint32_t ba[4] = {(uint32_t)bwk, (uint32_t)bhk, 1, (uint32_t)arows};
-    const uint64_t db[4] = {(uint64_t)w.W, (uint64_t)w.H, (uint64_t)w.B, (uint64_t)3 * w.Cin};
-    const uint32_t bbx[4] = {(uint32_t)bwk, (uint32_t)bhk, 1, (uint32_t)ntile};
+    const uint64_t nwb = (uint64_t)(w.W / bwk);
+    const uint64_t da[5] = {(uint64_t)bwk, (uint64_t)w.Cout, nwb, (uint64_t)w.H, (uint64_t)w.B};
+    const uint64_t sa[4] = {(uint64_t)bwk * 2, (uint64_t)w.Cout * bwk * 2, nwb * w.Cout * bwk * 2,
+                            (uint64_t)w.H * nwb * w.Cout * bwk * 2};
+    const uint32_t ba[5] = {(uint32_t)bwk, (uint32_t)arows, 1, 1, 1};
+    const uint64_t db[5] = {(uint64_t)bwk, (uint64_t)w.Cin, nwb, (uint64_t)w.H, (uint64_t)3 * w.B};
+    const uint64_t sb[4] = {(uint64_t)bwk * 2, (uint64_t)w.Cin * bwk * 2, nwb * w.Cin * bwk * 2,
+                            (uint64_t)w.H * nwb * w.Cin * bwk * 2};
+    const uint32_t bbx[5] = {(uint32_t)bwk, (uint32_t)ntile, 1, 1, 1};
     cudaError_t e;
-    if ((e = tensor_map(&ta, w.dyT, 4, da, sa, ba, kbytes)) != cudaSuccess) return e;
-    if ((e = tensor_map(&tb, w.xT3, 4, db, sa, bbx, kbytes)) != cudaSuccess) return e;
+    if ((e = tensor_map(&ta, w.dyT, 5, da, sa, ba, kbytes)) != cudaSuccess) return e;
+    if ((e = tensor_map(&tb, w.xT3, 5, db, sb, bbx, kbytes)) != cudaSuccess) return e;
     const dim3 grid((unsigned)((w.Cout + 127) / 128), (unsigned)(w.Cin / ntile), (unsigned)(9 * w.ksplit));
     return launch<MODE_WGRAD, EPI_ATOMIC>(ta, tb, p, grid, st);
 }

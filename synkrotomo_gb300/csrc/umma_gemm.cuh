@@ -7,14 +7,17 @@
 namespace synk {
 namespace unet {
 
-enum { MODE_GEMM = 0, MODE_CONV = 1, MODE_WGRAD = 2 };
+enum { MODE_GEMM = 0, MODE_CONV = 1, MODE_WGRAD = 2, MODE_HALO = 3 };
 enum { EPI_F32 = 0, EPI_BIAS_RELU = 1, EPI_MASK = 2, EPI_ATOMIC = 3, EPI_BIAS = 4 };
 
 struct GemmParams {
     int M, N, ncols, nk, kbytes, stages;
+    int gx, gy, gz;       // tile grid (x fastest); set by the launcher
+    long long ntiles;
     uint32_t bytesA, bytesB;
-    // MODE_CONV
+    // MODE_CONV / MODE_HALO
     int H, W, Cin, bw, bh, cchunks;
+    uint32_t aStage;      // MODE_HALO: bytes of the A strip in a stage (130 rows x 128 B, 1 KB aligned)
     // MODE_WGRAD
     int bwk, bhk, nb_w, nb_h, Bn, ksplit, mvalid;
     // epilogue

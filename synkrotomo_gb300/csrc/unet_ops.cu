@@ -14,145 +14,240 @@ namespace unet {
 __device__ __forceinline__ float bf(uint16_t x) { return __bfloat162float(__ushort_as_bfloat16(x)); }
 __device__ __forceinline__ uint16_t tobf(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
 
-// e[b,h,w,o] = relu(bias[o] + sum_tap x[b,h+dy,w+dx] * w[o][tap]), x FP32 1 channel.
-__global__ void first_conv_kernel(const float *__restrict__ x, const float *__restrict__ w,
-                                  const float *__restrict__ bias, uint16_t *__restrict__ y, int B, int H, int W,
-                                  int Cout, int ldy) {
-    const long long P = (long long)B * H * W;
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
-        const int w0 = (int)(p % W), h0 = (int)((p / W) % H);
-        const long long b = p / ((long long)W * H);
+// Eight BF16 channels travel as one 16-byte vector (channel strides and
+// offsets are multiples of 8, checked on the host).
+__device__ __forceinline__ void unpack8(const uint4 u, float (&f)[8]) {
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        f[2 * i] = __uint_as_float(w[i] << 16);
+        f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+    }
+}
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = (uint32_t)tobf(f[2 * i]) | ((uint32_t)tobf(f[2 * i + 1]) << 16);
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+__device__ __forceinline__ uint4 ld8(const uint16_t *p) { return *reinterpret_cast<const uint4 *>(p); }
+__device__ __forceinline__ void st8(uint16_t *p, uint4 v) { *reinterpret_cast<uint4 *>(p) = v; }
+
+// e[b,h,w,o] = relu(bias[o] + sum_tap x[b,h+dy,w+dx] * w[o][tap]), x FP32 1
+// channel; one thread per pixel, all Cout (<= 64, multiple of 8) outputs.
+__global__ void __launch_bounds__(256) first_conv_kernel(const float *__restrict__ x, const float *__restrict__ w,
+                                                         const float *__restrict__ bias, uint16_t *__restrict__ y,
+                                                         int B, int H, int W, int Cout, int ldy) {
+    __shared__ float sw[64 * 9], sb[64];
+    for (int i = threadIdx.x; i < Cout * 9; i += blockDim.x) sw[i] = w[i];
+    for (int i = threadIdx.x; i < Cout; i += blockDim.x) sb[i] = bias[i];
+    __syncthreads();
+    const unsigned P = (unsigned)B * H * W;
+    for (unsigned p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const unsigned w0 = p % W, t = p / W, h0 = t % H;
         float v[9];
 #pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const int h = h0 + t / 3 - 1, ww = w0 + t % 3 - 1;
-            v[t] = (h >= 0 && h < H && ww >= 0 && ww < W) ? x[(b * H + h) * W + ww] : 0.0f;
+        for (int k = 0; k < 9; ++k) {
+            const int h = (int)h0 + k / 3 - 1, ww = (int)w0 + k % 3 - 1;
+            v[k] = (h >= 0 && h < H && ww >= 0 && ww < W) ? __ldg(x + (long long)p + (k / 3 - 1) * W + (k % 3 - 1))
+                                                          : 0.0f;
         }
-        uint16_t *o = y + p * ldy;
-        for (int c = 0; c < Cout; ++c) {
-            float s = bias[c];
+        uint16_t *o = y + (long long)p * ldy;
+        for (int c0 = 0; c0 < Cout; c0 += 8) {
+            float r[8];
 #pragma unroll
-            for (int t = 0; t < 9; ++t) s = fmaf(v[t], w[c * 9 + t], s);
-            o[c] = tobf(fmaxf(s, 0.0f));
+            for (int j = 0; j < 8; ++j) {
+                float s = sb[c0 + j];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) s = fmaf(v[k], sw[(c0 + j) * 9 + k], s);
+                r[j] = fmaxf(s, 0.0f);
+            }
+            st8(o + c0, pack8(r));
         }
     }
 }
 
-// dw[o][tap] += sum_p dz[p][o] * x[p + tap]; db[o] += sum_p dz[p][o].  One block
-// per (o, slice of pixels); shared-memory reduction, one atomic per block.
-__global__ void first_conv_wgrad_kernel(const float *__restrict__ x, const uint16_t *__restrict__ dz, int ldz,
-                                        float *__restrict__ dw, float *__restrict__ db, int B, int H, int W) {
-    const int o = blockIdx.y;
-    const long long P = (long long)B * H * W;
-    float acc[10] = {0};
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
-        const float g = bf(dz[p * ldz + o]);
-        if (g == 0.0f) continue;
-        const int w0 = (int)(p % W), h0 = (int)((p / W) % H);
-        const long long b = p / ((long long)W * H);
+// dw[o][tap] += sum_p dz[p][o] * x[p + tap]; db[o] += sum_p dz[p][o], Cout = 32.
+// Thread (pixel, group of 8 channels); lanes with the same group reduce by
+// shuffles, warps through shared memory, one atomic per (o, tap) per block.
+__global__ void __launch_bounds__(256) first_conv_wgrad_kernel(const float *__restrict__ x,
+                                                               const uint16_t *__restrict__ dz, int ldz,
+                                                               float *__restrict__ dw, float *__restrict__ db, int B,
+                                                               int H, int W) {
+    const int grp = threadIdx.x & 3;                    // channels 8*grp .. +7
+    const unsigned P = (unsigned)B * H * W;
+    float acc[8][10];
 #pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const int h = h0 + t / 3 - 1, ww = w0 + t % 3 - 1;
-            if (h >= 0 && h < H && ww >= 0 && ww < W) acc[t] = fmaf(g, x[(b * H + h) * W + ww], acc[t]);
+    for (int j = 0; j < 8; ++j)
+#pragma unroll
+        for (int k = 0; k < 10; ++k) acc[j][k] = 0.0f;
+    const unsigned stride = gridDim.x * (blockDim.x >> 2);
+    for (unsigned p = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2); p < P; p += stride) {
+        float g[8];
+        unpack8(ld8(dz + (long long)p * ldz + 8 * grp), g);
+        const unsigned w0 = p % W, t = p / W, h0 = t % H;
+        float v[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const int h = (int)h0 + k / 3 - 1, ww = (int)w0 + k % 3 - 1;
+            v[k] = (h >= 0 && h < H && ww >= 0 && ww < W) ? __ldg(x + (long long)p + (k / 3 - 1) * W + (k % 3 - 1))
+                                                          : 0.0f;
         }
-        acc[9] += g;
-    }
-    __shared__ float sh[10][256];
 #pragma unroll
-    for (int t = 0; t < 10; ++t) sh[t][threadIdx.x] = acc[t];
+        for (int j = 0; j < 8; ++j) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) acc[j][k] = fmaf(g[j], v[k], acc[j][k]);
+            acc[j][9] += g[j];
+        }
+    }
+    __shared__ float red[8][4][80];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+#pragma unroll
+        for (int k = 0; k < 10; ++k) {
+            float a = acc[j][k];
+            a += __shfl_xor_sync(0xffffffffu, a, 4);
+            a += __shfl_xor_sync(0xffffffffu, a, 8);
+            a += __shfl_xor_sync(0xffffffffu, a, 16);
+            if (lane < 4) red[warp][lane][j * 10 + k] = a;
+        }
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s)
-            for (int t = 0; t < 10; ++t) sh[t][threadIdx.x] += sh[t][threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x < 9) atomicAdd(dw + o * 9 + threadIdx.x, sh[threadIdx.x][0]);
-    if (threadIdx.x == 9) atomicAdd(db + o, sh[9][0]);
-}
-
-// out[b,h,w,c] = max of the 2x2 block of in (H, W of the input).
-__global__ void maxpool_kernel(const uint16_t *__restrict__ in, int ldi, int ioff, uint16_t *__restrict__ out, int ldo,
-                               int B, int H, int W, int C) {
-    const int Ho = H / 2, Wo = W / 2;
-    const long long n = (long long)B * Ho * Wo * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long q = i / C;
-        const int wo = (int)(q % Wo), ho = (int)((q / Wo) % Ho);
-        const long long b = q / ((long long)Wo * Ho);
-        const long long r0 = (b * H + 2 * ho) * W + 2 * wo;
-        const float a0 = bf(in[r0 * ldi + ioff + c]), a1 = bf(in[(r0 + 1) * ldi + ioff + c]);
-        const float a2 = bf(in[(r0 + W) * ldi + ioff + c]), a3 = bf(in[(r0 + W + 1) * ldi + ioff + c]);
-        out[q * ldo + c] = tobf(fmaxf(fmaxf(a0, a1), fmaxf(a2, a3)));
+    for (int i = threadIdx.x; i < 320; i += blockDim.x) {
+        const int gg = i / 80, jk = i - gg * 80;
+        float s = 0.0f;
+        for (int wi = 0; wi < (int)(blockDim.x >> 5); ++wi) s += red[wi][gg][jk];
+        const int o = 8 * gg + jk / 10, k = jk % 10;
+        atomicAdd(k < 9 ? dw + o * 9 + k : db + o, s);
     }
 }
 
-// dE[b,h,w,c] (+)= dP[b,h/2,w/2,c] where (h,w) holds the block's max (first in
-// scan order), plus the skip gradient dS[b,h,w,c] when given.
-__global__ void maxpool_bwd_kernel(const uint16_t *__restrict__ e, int lde, int eoff, const uint16_t *__restrict__ dp,
-                                   int ldp, const uint16_t *__restrict__ ds, int lds, int soff,
-                                   uint16_t *__restrict__ de, int ldd, int B, int H, int W, int C) {
-    const long long n = (long long)B * H * W * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long q = i / C;
-        const int w = (int)(q % W), h = (int)((q / W) % H);
-        const long long b = q / ((long long)W * H);
-        const int hb = h & ~1, wb = w & ~1;
-        const long long r0 = (b * H + hb) * W + wb;
-        const float a[4] = {bf(e[r0 * lde + eoff + c]), bf(e[(r0 + 1) * lde + eoff + c]),
-                            bf(e[(r0 + W) * lde + eoff + c]), bf(e[(r0 + W + 1) * lde + eoff + c])};
-        int am = 0;
-        for (int t = 1; t < 4; ++t)
-            if (a[t] > a[am]) am = t;
-        const int me = (h - hb) * 2 + (w - wb);
-        float g = 0.0f;
-        if (me == am) g = bf(dp[((b * (H / 2) + h / 2) * (W / 2) + w / 2) * ldp + c]);
-        if (ds) g += bf(ds[q * lds + soff + c]);
-        de[q * ldd + c] = tobf(g);
+// out[b,h,w,c] = max of the 2x2 block of in (H, W of the input); thread =
+// (output pixel, 8 channels).
+__global__ void __launch_bounds__(256) maxpool_kernel(const uint16_t *__restrict__ in, int ldi, int ioff,
+                                                      uint16_t *__restrict__ out, int ldo, int B, int H, int W, int C) {
+    const unsigned Ho = H / 2, Wo = W / 2, G = C / 8;
+    const unsigned n = (unsigned)B * Ho * Wo * G;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned g = i % G, q = i / G;
+        const unsigned wo = q % Wo, t = q / Wo, ho = t % Ho, b = t / Ho;
+        const long long r0 = ((long long)b * H + 2 * ho) * W + 2 * wo;
+        const int c = ioff + 8 * (int)g;
+        float a0[8], a1[8], a2[8], a3[8];
+        unpack8(ld8(in + r0 * ldi + c), a0);
+        unpack8(ld8(in + (r0 + 1) * ldi + c), a1);
+        unpack8(ld8(in + (r0 + W) * ldi + c), a2);
+        unpack8(ld8(in + (r0 + W + 1) * ldi + c), a3);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a0[j] = fmaxf(fmaxf(a0[j], a1[j]), fmaxf(a2[j], a3[j]));
+        st8(out + (long long)q * ldo + 8 * g, pack8(a0));
     }
 }
 
-// out[b,h,w,ooff+c] = in[b,h/2,w/2,c] (output H, W).
-__global__ void upsample_kernel(const uint16_t *__restrict__ in, int ldi, uint16_t *__restrict__ out, int ldo,
-                                int ooff, int B, int H, int W, int C) {
-    const long long n = (long long)B * H * W * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long q = i / C;
-        const int w = (int)(q % W), h = (int)((q / W) % H);
-        const long long b = q / ((long long)W * H);
-        out[q * ldo + ooff + c] = in[((b * (H / 2) + h / 2) * (W / 2) + w / 2) * ldi + c];
+// dE[b,h,w,c] = dP[b,h/2,w/2,c] where (h,w) holds the block's max (first in
+// scan order), plus the skip gradient dS[b,h,w,c] when given; thread =
+// (pooled pixel, 8 channels), writing its 2x2 block.
+__global__ void __launch_bounds__(256) maxpool_bwd_kernel(const uint16_t *__restrict__ e, int lde, int eoff,
+                                                          const uint16_t *__restrict__ dp, int ldp,
+                                                          const uint16_t *__restrict__ ds, int lds, int soff,
+                                                          uint16_t *__restrict__ de, int ldd, int B, int H, int W,
+                                                          int C) {
+    const unsigned Ho = H / 2, Wo = W / 2, G = C / 8;
+    const unsigned n = (unsigned)B * Ho * Wo * G;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned g = i % G, q = i / G;
+        const unsigned wo = q % Wo, t = q / Wo, ho = t % Ho, b = t / Ho;
+        const long long r0 = ((long long)b * H + 2 * ho) * W + 2 * wo;
+        const long long rr[4] = {r0, r0 + 1, r0 + W, r0 + W + 1};
+        float a[4][8], gp[8];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) unpack8(ld8(e + rr[k] * lde + eoff + 8 * g), a[k]);
+        unpack8(ld8(dp + (long long)q * ldp + 8 * g), gp);
+        float o[4][8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            int am = 0;
+            float best = a[0][j];
+#pragma unroll
+            for (int k = 1; k < 4; ++k)
+                if (a[k][j] > best) {
+                    best = a[k][j];
+                    am = k;
+                }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) o[k][j] = (k == am) ? gp[j] : 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (ds) {
+                float sk[8];
+                unpack8(ld8(ds + rr[k] * lds + soff + 8 * g), sk);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) o[k][j] += sk[j];
+            }
+            st8(de + rr[k] * ldd + 8 * g, pack8(o[k]));
+        }
     }
 }
 
-// out[b,h,w,c] = sum of the 2x2 children in[b,2h+i,2w+j,ioff+c] (output H, W).
-__global__ void upsample_bwd_kernel(const uint16_t *__restrict__ in, int ldi, int ioff, uint16_t *__restrict__ out,
-                                    int ldo, int B, int H, int W, int C) {
-    const long long n = (long long)B * H * W * C;
+// out[b,h,w,ooff+c] = in[b,h/2,w/2,c] (output H, W); thread = (output pixel, 8 channels).
+__global__ void __launch_bounds__(256) upsample_kernel(const uint16_t *__restrict__ in, int ldi,
+                                                       uint16_t *__restrict__ out, int ldo, int ooff, int B, int H,
+                                                       int W, int C) {
+    const unsigned G = C / 8;
+    const unsigned n = (unsigned)B * H * W * G;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned g = i % G, q = i / G;
+        const unsigned w = q % W, t = q / W, h = t % H, b = t / H;
+        const long long src = ((long long)b * (H / 2) + h / 2) * (W / 2) + w / 2;
+        st8(out + (long long)q * ldo + ooff + 8 * g, ld8(in + src * ldi + 8 * g));
+    }
+}
+
+// out[b,h,w,c] = sum of the 2x2 children in[b,2h+i,2w+j,ioff+c] (output H, W);
+// thread = (output pixel, 8 channels).
+__global__ void __launch_bounds__(256) upsample_bwd_kernel(const uint16_t *__restrict__ in, int ldi, int ioff,
+                                                           uint16_t *__restrict__ out, int ldo, int B, int H, int W,
+                                                           int C) {
+    const unsigned G = C / 8;
+    const unsigned n = (unsigned)B * H * W * G;
     const int W2 = 2 * W;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long q = i / C;
-        const int w = (int)(q % W), h = (int)((q / W) % H);
-        const long long b = q / ((long long)W * H);
-        const long long r0 = (b * 2 * H + 2 * h) * W2 + 2 * w;
-        const float s = bf(in[r0 * ldi + ioff + c]) + bf(in[(r0 + 1) * ldi + ioff + c]) +
-                        bf(in[(r0 + W2) * ldi + ioff + c]) + bf(in[(r0 + W2 + 1) * ldi + ioff + c]);
-        out[q * ldo + c] = tobf(s);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned g = i % G, q = i / G;
+        const unsigned w = q % W, t = q / W, h = t % H, b = t / H;
+        const long long r0 = ((long long)b * 2 * H + 2 * h) * W2 + 2 * w;
+        const int c = ioff + 8 * (int)g;
+        float s0[8], s1[8], s2[8], s3[8];
+        unpack8(ld8(in + r0 * ldi + c), s0);
+        unpack8(ld8(in + (r0 + 1) * ldi + c), s1);
+        unpack8(ld8(in + (r0 + W2) * ldi + c), s2);
+        unpack8(ld8(in + (r0 + W2 + 1) * ldi + c), s3);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s0[j] = s0[j] + s1[j] + s2[j] + s3[j];
+        st8(out + (long long)q * ldo + 8 * g, pack8(s0));
     }
 }
 
-// Output head and loss: y = x0 + bh + sum_c wh[c] * d[p][c]; with a target,
-// g = 2 (y - t) / P and loss += (y - t)^2 / P (FP64).
-__global__ void head_kernel(const float *__restrict__ x0, const uint16_t *__restrict__ d, int ldd,
-                            const float *__restrict__ wh, const float *__restrict__ bh, float *__restrict__ y,
-                            const float *__restrict__ target, float *__restrict__ g, double *__restrict__ loss,
-                            long long P, int C) {
+// Output head and loss: y = x0 + bh + sum_c wh[c] * d[p][c] (C <= 64, multiple
+// of 8); with a target, g = 2 (y - t) / P and loss += (y - t)^2 / P (FP64).
+__global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ x0, const uint16_t *__restrict__ d,
+                                                   int ldd, const float *__restrict__ wh, const float *__restrict__ bh,
+                                                   float *__restrict__ y, const float *__restrict__ target,
+                                                   float *__restrict__ g, double *__restrict__ loss, long long P,
+                                                   int C) {
+    __shared__ float sw[64];
+    for (int i = threadIdx.x; i < C; i += blockDim.x) sw[i] = wh[i];
+    __syncthreads();
     double l = 0.0;
+    const float b0 = bh[0];
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
-        float s = x0[p] + bh[0];
-        for (int c = 0; c < C; ++c) s = fmaf(wh[c], bf(d[p * ldd + c]), s);
+        float s = x0[p] + b0;
+        for (int c0 = 0; c0 < C; c0 += 8) {
+            float dv[8];
+            unpack8(ld8(d + p * ldd + c0), dv);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s = fmaf(sw[c0 + j], dv[j], s);
+        }
         if (y) y[p] = s;
         if (target) {
             const float r = s - target[p];
@@ -161,102 +256,135 @@ __global__ void head_kernel(const float *__restrict__ x0, const uint16_t *__rest
         }
     }
     if (!target) return;
-    __shared__ double sh[256];
-    sh[threadIdx.x] = l;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    __shared__ double sh[8];
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = l;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+        atomicAdd(loss, t / (double)P);
     }
-    if (threadIdx.x == 0) atomicAdd(loss, sh[0] / (double)P);
 }
 
-// Head backward: dz[p][c] = g[p] * wh[c] * (d[p][c] > 0); dwh[c] += sum_p g d; dbh += sum g.
-__global__ void head_bwd_kernel(const float *__restrict__ g, const uint16_t *__restrict__ d, int ldd,
-                                const float *__restrict__ wh, uint16_t *__restrict__ dz, int ldz,
-                                float *__restrict__ dwh, float *__restrict__ dbh, long long P, int C) {
+// Head backward (C = 32): dz[p][c] = g[p] * wh[c] * (d[p][c] > 0);
+// dwh[c] += sum_p g d; dbh += sum g.
+__global__ void __launch_bounds__(256) head_bwd_kernel(const float *__restrict__ g, const uint16_t *__restrict__ d,
+                                                       int ldd, const float *__restrict__ wh,
+                                                       uint16_t *__restrict__ dz, int ldz, float *__restrict__ dwh,
+                                                       float *__restrict__ dbh, long long P, int C) {
+    __shared__ float sw[32];
+    __shared__ float red[8][33];
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) sw[i] = i < C ? wh[i] : 0.0f;
+    __syncthreads();
     float acc[33];
-    for (int c = 0; c <= C; ++c) acc[c] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 33; ++c) acc[c] = 0.0f;
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
         const float gp = g[p];
-        for (int c = 0; c < C; ++c) {
-            const float dv = bf(d[p * ldd + c]);
-            dz[p * ldz + c] = tobf(dv > 0.0f ? gp * wh[c] : 0.0f);
-            acc[c] = fmaf(gp, dv, acc[c]);
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 8) {
+            float dv[8], o[8];
+            unpack8(ld8(d + p * ldd + c0), dv);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                o[j] = dv[j] > 0.0f ? gp * sw[c0 + j] : 0.0f;
+                acc[c0 + j] = fmaf(gp, dv[j], acc[c0 + j]);
+            }
+            st8(dz + p * ldz + c0, pack8(o));
         }
-        acc[C] += gp;
+        acc[32] += gp;
     }
-    __shared__ float sh[256];
-    for (int c = 0; c <= C; ++c) {
-        sh[threadIdx.x] = acc[c];
-        __syncthreads();
-        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-            if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) atomicAdd(c < C ? dwh + c : dbh, sh[0]);
-        __syncthreads();
-    }
-}
-
-// Channel-major copies for the weight gradient.  mode 0: out[c][p] = in[p][c]
-// (one copy); mode 1: three copies out[k][c][b][h][w] = in[b][h][w+k-1][c]
-// (zero outside the image).  32 x 32 (pixel, channel) tiles through shared memory.
-__global__ void to_cmajor_kernel(const uint16_t *__restrict__ in, int ldi, int ioff, uint16_t *__restrict__ out,
-                                 int C, long long P, int W, int shifted) {
-    __shared__ uint16_t tile[32][34];
-    const long long p0 = (long long)blockIdx.x * 32;
-    const int c0 = blockIdx.y * 32;
-    for (int i = threadIdx.y; i < 32; i += 8) {
-        const long long p = p0 + i;
-        const int c = c0 + threadIdx.x;
-        tile[i][threadIdx.x] = (p < P && c < C) ? in[p * ldi + ioff + c] : (uint16_t)0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < 33; ++c) {
+        float a = acc[c];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) red[warp][c] = a;
     }
     __syncthreads();
-    for (int i = threadIdx.y; i < 32; i += 8) {
-        const int c = c0 + i;
-        const long long p = p0 + threadIdx.x;
-        if (c >= C || p >= P) continue;
-        const uint16_t v = tile[threadIdx.x][i];
-        if (!shifted) {
-            out[(long long)c * P + p] = v;
-        } else {
-            // value at pixel p lands at p+1 in copy 0 (x[w-1]), p in copy 1, p-1 in copy 2
-            const int w = (int)(p % W);
-            out[(long long)(C + c) * P + p] = v;
-            if (w + 1 < W) out[(long long)c * P + p + 1] = v;
-            if (w >= 1) out[(long long)(2 * C + c) * P + p - 1] = v;
-        }
-    }
-}
-
-// Borders of the shifted copies: copy 0 at w = 0 and copy 2 at w = W-1 are zero.
-__global__ void shift_border_kernel(uint16_t *__restrict__ out, int C, long long P, int W) {
-    const long long rows = P / W;
-    const long long n = rows * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long r = i / C;
-        out[(long long)c * P + r * W] = 0;
-        out[(long long)(2 * C + c) * P + r * W + W - 1] = 0;
-    }
-}
-
-// db[c] += sum_p dz[p][c]
-__global__ void bias_grad_kernel(const uint16_t *__restrict__ dz, int ldz, float *__restrict__ db, long long P, int C) {
-    const int c = blockIdx.y * 32 + (threadIdx.x & 31);
-    float acc = 0.0f;
-    if (c < C)
-        for (long long p = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; p < P;
-             p += (long long)gridDim.x * (blockDim.x / 32))
-            acc += bf(dz[p * ldz + c]);
-    __shared__ float sh[8][33];
-    sh[threadIdx.x / 32][threadIdx.x & 31] = acc;
-    __syncthreads();
-    if (threadIdx.x < 32) {
+    if (threadIdx.x < 33 && (threadIdx.x < (unsigned)C || threadIdx.x == 32)) {
         float s = 0.0f;
-        for (int i = 0; i < (int)blockDim.x / 32; ++i) s += sh[i][threadIdx.x];
-        if (c < C) atomicAdd(db + c, s);
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i][threadIdx.x];
+        atomicAdd(threadIdx.x < 32 ? dwh + threadIdx.x : dbh, s);
+    }
+}
+
+// Blocked copies for the weight gradient: pixel chunks of cw pixels of one
+// image row (cw = 64 when W >= 64, else 32), each chunk stored as [C][cw].
+// shifted = 0: out[q][c][j] = in[q*cw + j][c] (one copy); shifted = 1: three
+// copies, copy k at k*P*C, holding in[p + k - 1][c] when pixel p+k-1 is in
+// p's image row (w+k-1 in [0, W)), else 0.  A block transposes 64 pixels x 64
+// channels through shared memory (plus one halo pixel on each side), reading
+// 16-byte vectors and writing pixel pairs; the writes of a chunk are contiguous.
+__global__ void __launch_bounds__(256) to_cmajor_kernel(const uint16_t *__restrict__ in, int ldi, int ioff,
+                                                        uint16_t *__restrict__ out, int C, long long P, int W,
+                                                        int shifted) {
+    __shared__ __align__(16) uint16_t tile[66][72];   // [pixel p0-1 .. p0+64][channel], rows padded
+    const long long p0 = (long long)blockIdx.x * 64;
+    const int c0 = blockIdx.y * 64;
+    const int cw = W >= 64 ? 64 : 32;
+    const int cn = min(64, C - c0);     // multiple of 8
+    for (int i = threadIdx.x; i < 66 * 8; i += blockDim.x) {
+        const int r = i >> 3, g = i & 7;
+        const long long p = p0 - 1 + r;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (8 * g < cn && p >= 0 && p < P) v = ld8(in + p * ldi + ioff + c0 + 8 * g);
+        *reinterpret_cast<uint4 *>(&tile[r][8 * g]) = v;
+    }
+    __syncthreads();
+    const int ncopies = shifted ? 3 : 1;
+    // thread = (channel, pixel pair); 32 pairs per channel
+    for (int i = threadIdx.x; i < cn * 32; i += blockDim.x) {
+        const int c = i >> 5, pr = (i & 31) * 2;
+        const long long p = p0 + pr;       // even; p and p+1 share a chunk (cw even)
+        if (p >= P) continue;
+        const int w0 = (int)(p % W);
+        const int wp[2] = {w0, w0 + 1 == W ? 0 : w0 + 1};
+        const long long q = p / cw;
+        const int j = (int)(p - q * cw);
+        for (int k = 0; k < ncopies; ++k) {
+            const int dsh = shifted ? k - 1 : 0;
+            uint16_t v[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int w = wp[e];
+                const bool in_row = w + dsh >= 0 && w + dsh < W;
+                v[e] = in_row ? tile[pr + e + 1 + dsh][c] : (uint16_t)0;
+            }
+            uint16_t *o = out + (long long)k * P * C + (q * C + c0 + c) * cw + j;
+            *reinterpret_cast<uint32_t *>(o) = (uint32_t)v[0] | ((uint32_t)v[1] << 16);
+        }
+    }
+}
+
+// db[c] += sum_p dz[p][c].  Thread = (channel group g of 8, pixel lane): a block
+// covers G = C/8 groups x 256/G pixel lanes, 16-byte loads; lanes of one
+// group are summed in shared memory, one atomic per channel per block.
+__global__ void __launch_bounds__(256) bias_grad_kernel(const uint16_t *__restrict__ dz, int ldz,
+                                                        float *__restrict__ db, long long P, int C) {
+    const int G = C / 8;
+    const int lanes = blockDim.x / G;                  // pixel lanes per block
+    const int g = threadIdx.x % G, pl = threadIdx.x / G;
+    float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (pl < lanes)
+        for (long long p = (long long)blockIdx.x * lanes + pl; p < P; p += (long long)gridDim.x * lanes) {
+            float v[8];
+            unpack8(ld8(dz + p * ldz + 8 * g), v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] += v[j];
+        }
+    __shared__ float sh[256][9];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) sh[threadIdx.x][j] = pl < lanes ? acc[j] : 0.0f;
+    __syncthreads();
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        const int gg = c / 8, j = c % 8;
+        float t = 0.0f;
+        for (int l = 0; l < lanes; ++l) t += sh[l * G + gg][j];
+        atomicAdd(db + c, t);
     }
 }
 
@@ -305,60 +433,72 @@ static unsigned grid_for(long long n, int threads = 256) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
+static bool v8(int a) { return (a & 7) == 0; }
+
 cudaError_t first_conv(const float *x, const float *w, const float *b, uint16_t *y, int B, int H, int W, int Cout,
                        int ldy, cudaStream_t st) {
+    if (!v8(Cout) || Cout > 64 || !v8(ldy) || (long long)B * H * W >= (1LL << 31)) return cudaErrorInvalidValue;
     first_conv_kernel<<<grid_for((long long)B * H * W), 256, 0, st>>>(x, w, b, y, B, H, W, Cout, ldy);
     return cudaGetLastError();
 }
 cudaError_t first_conv_wgrad(const float *x, const uint16_t *dz, int ldz, float *dw, float *db, int B, int H, int W,
                              int Cout, cudaStream_t st) {
-    dim3 grid(64, Cout);
-    first_conv_wgrad_kernel<<<grid, 256, 0, st>>>(x, dz, ldz, dw, db, B, H, W);
+    if (Cout != 32 || !v8(ldz) || (long long)B * H * W >= (1LL << 31)) return cudaErrorInvalidValue;
+    first_conv_wgrad_kernel<<<152 * 2, 256, 0, st>>>(x, dz, ldz, dw, db, B, H, W);
     return cudaGetLastError();
 }
 cudaError_t maxpool(const uint16_t *in, int ldi, int ioff, uint16_t *out, int ldo, int B, int H, int W, int C,
                     cudaStream_t st) {
-    maxpool_kernel<<<grid_for((long long)B * H * W * C / 4), 256, 0, st>>>(in, ldi, ioff, out, ldo, B, H, W, C);
+    const long long n = (long long)B * (H / 2) * (W / 2) * (C / 8);
+    if (!v8(C) || !v8(ldi) || !v8(ioff) || !v8(ldo) || n >= (1LL << 31)) return cudaErrorInvalidValue;
+    maxpool_kernel<<<grid_for(n), 256, 0, st>>>(in, ldi, ioff, out, ldo, B, H, W, C);
     return cudaGetLastError();
 }
 cudaError_t maxpool_bwd(const uint16_t *e, int lde, int eoff, const uint16_t *dp, int ldp, const uint16_t *ds,
                         int lds, int soff, uint16_t *de, int ldd, int B, int H, int W, int C, cudaStream_t st) {
-    maxpool_bwd_kernel<<<grid_for((long long)B * H * W * C), 256, 0, st>>>(e, lde, eoff, dp, ldp, ds, lds, soff, de,
-                                                                          ldd, B, H, W, C);
+    const long long n = (long long)B * (H / 2) * (W / 2) * (C / 8);
+    if (!v8(C) || !v8(lde) || !v8(eoff) || !v8(ldp) || !v8(lds) || !v8(soff) || !v8(ldd) || n >= (1LL << 31))
+        return cudaErrorInvalidValue;
+    maxpool_bwd_kernel<<<grid_for(n), 256, 0, st>>>(e, lde, eoff, dp, ldp, ds, lds, soff, de, ldd, B, H, W, C);
     return cudaGetLastError();
 }
 cudaError_t upsample(const uint16_t *in, int ldi, uint16_t *out, int ldo, int ooff, int B, int H, int W, int C,
                      cudaStream_t st) {
-    upsample_kernel<<<grid_for((long long)B * H * W * C), 256, 0, st>>>(in, ldi, out, ldo, ooff, B, H, W, C);
+    const long long n = (long long)B * H * W * (C / 8);
+    if (!v8(C) || !v8(ldi) || !v8(ldo) || !v8(ooff) || n >= (1LL << 31)) return cudaErrorInvalidValue;
+    upsample_kernel<<<grid_for(n), 256, 0, st>>>(in, ldi, out, ldo, ooff, B, H, W, C);
     return cudaGetLastError();
 }
 cudaError_t upsample_bwd(const uint16_t *in, int ldi, int ioff, uint16_t *out, int ldo, int B, int H, int W, int C,
                          cudaStream_t st) {
-    upsample_bwd_kernel<<<grid_for((long long)B * H * W * C), 256, 0, st>>>(in, ldi, ioff, out, ldo, B, H, W, C);
+    const long long n = (long long)B * H * W * (C / 8);
+    if (!v8(C) || !v8(ldi) || !v8(ioff) || !v8(ldo) || n >= (1LL << 31)) return cudaErrorInvalidValue;
+    upsample_bwd_kernel<<<grid_for(n), 256, 0, st>>>(in, ldi, ioff, out, ldo, B, H, W, C);
     return cudaGetLastError();
 }
 cudaError_t head(const float *x0, const uint16_t *d, int ldd, const float *wh, const float *bh, float *y,
                  const float *target, float *g, double *loss, long long P, int C, cudaStream_t st) {
+    if (!v8(C) || C > 64 || !v8(ldd)) return cudaErrorInvalidValue;
     head_kernel<<<grid_for(P), 256, 0, st>>>(x0, d, ldd, wh, bh, y, target, g, loss, P, C);
     return cudaGetLastError();
 }
 cudaError_t head_bwd(const float *g, const uint16_t *d, int ldd, const float *wh, uint16_t *dz, int ldz, float *dwh,
                      float *dbh, long long P, int C, cudaStream_t st) {
-    head_bwd_kernel<<<grid_for(P), 256, 0, st>>>(g, d, ldd, wh, dz, ldz, dwh, dbh, P, C);
+    if (C != 32 || !v8(ldd) || !v8(ldz)) return cudaErrorInvalidValue;
+    head_bwd_kernel<<<152 * 4, 256, 0, st>>>(g, d, ldd, wh, dz, ldz, dwh, dbh, P, C);
     return cudaGetLastError();
 }
 cudaError_t to_cmajor(const uint16_t *in, int ldi, int ioff, uint16_t *out, int C, long long P, int W, int shifted,
                       cudaStream_t st) {
-    dim3 grid((unsigned)((P + 31) / 32), (unsigned)((C + 31) / 32));
-    to_cmajor_kernel<<<grid, dim3(32, 8), 0, st>>>(in, ldi, ioff, out, C, P, W, shifted);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || !shifted) return e;
-    shift_border_kernel<<<grid_for(P / W * C), 256, 0, st>>>(out, C, P, W);
+    if (!v8(C) || !v8(ldi) || !v8(ioff) || W < 32 || W % (W >= 64 ? 64 : 32) || P % W)
+        return cudaErrorInvalidValue;
+    dim3 grid((unsigned)((P + 63) / 64), (unsigned)((C + 63) / 64));
+    to_cmajor_kernel<<<grid, 256, 0, st>>>(in, ldi, ioff, out, C, P, W, shifted);
     return cudaGetLastError();
 }
 cudaError_t bias_grad(const uint16_t *dz, int ldz, float *db, long long P, int C, cudaStream_t st) {
-    dim3 grid(256, (unsigned)((C + 31) / 32));
-    bias_grad_kernel<<<grid, 256, 0, st>>>(dz, ldz, db, P, C);
+    if (!v8(C) || C > 2048 || !v8(ldz)) return cudaErrorInvalidValue;
+    bias_grad_kernel<<<152 * 2, 256, 0, st>>>(dz, ldz, db, P, C);
     return cudaGetLastError();
 }
 cudaError_t adam(float *w, float *g, float *m, float *v, long long n, float lr, float b1, float b2, float eps, int step,

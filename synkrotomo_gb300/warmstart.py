@@ -23,7 +23,6 @@ import json
 import math
 import time
 
-import numpy as np
 import torch
 
 from . import phantom
@@ -98,18 +97,34 @@ def make_dataset(prob: Problem, n: int, seed: int, target_iters: int = 1000, chu
     return torch.cat(xs), torch.cat(ts)
 
 
+def lr_at(step: int, total: int, lr: float, warmup: int = 100, floor: float = 0.02) -> float:
+    """Learning rate of a step: linear warm-up to lr over `warmup` steps, then
+    cosine decay to floor*lr at the last step."""
+    if step < warmup:
+        return lr * (step + 1) / warmup
+    t = (step - warmup) / max(1, total - warmup)
+    return lr * (floor + (1.0 - floor) * 0.5 * (1.0 + math.cos(math.pi * min(1.0, t))))
+
+
 def train(net: UNet, inputs: torch.Tensor, targets: torch.Tensor, epochs: int, batch: int = 32, lr: float = 1e-3,
-          seed: int = 0, log=None):
+          seed: int = 0, log=None, schedule: bool = True):
+    """Adam on the MSE loss, mini-batches drawn without replacement each
+    epoch; peak learning rate lr with warm-up and cosine decay (schedule=True)
+    or constant.  Returns the mean loss of each epoch."""
     n = inputs.shape[0]
     N = net.size
     hist = []
     g = torch.Generator(device="cpu").manual_seed(seed)
+    total = epochs * (n // batch)
+    step = 0
     for ep in range(epochs):
         perm = torch.randperm(n, generator=g)
         losses = []
         for i in range(0, n - batch + 1, batch):
             idx = perm[i:i + batch].cuda()
-            loss = net.train_step(inputs[idx].view(batch, N, N), targets[idx].view(batch, N, N), lr=lr)
+            lr_s = lr_at(step, total, lr, warmup=max(1, min(100, total // 10))) if schedule else lr
+            step += 1
+            loss = net.train_step(inputs[idx].view(batch, N, N), targets[idx].view(batch, N, N), lr=lr_s)
             losses.append(loss.clone())
         ep_loss = float(torch.stack(losses).mean().item())
         hist.append(ep_loss)
@@ -190,22 +205,6 @@ def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 1
             "fallback_images": int(fallback.sum().item()), "rows": rows}
 
 
-def oracle_check(net: UNet, prob: Problem, seed: int, iterations: int = 30) -> dict:
-    """Warm-started GPU SIRT against the FP64 oracle's SIRT from the same
-    start (one held-out image; test-infrastructure oracle, CPU)."""
-    from oracle import fut_ref
-    imgs = ellipse_batch(1, prob.size, seed)
-    b = prob.sinograms(imgs, seed)
-    x1, _, _ = prob.sirt(b, 1)
-    x0 = net.forward(x1.view(1, prob.size, prob.size)).view(1, -1)
-    xg, _, _ = prob.sirt(b, iterations, start=x0)
-    g = prob.g
-    ops = fut_ref.SirtOperators(g.angles, g.rhozero, g.deltarho, g.numrhos, prob.size)
-    x64 = ops.iterate(x0.view(-1).cpu().numpy(), b.view(-1).cpu().numpy(), iterations)
-    xg = xg.view(-1).cpu().double().numpy()
-    return {"iterations": iterations, "rel_l2_vs_fp64": float(np.linalg.norm(xg - x64) / np.linalg.norm(x64))}
-
-
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--train", type=int, default=20000)
@@ -216,11 +215,11 @@ def main(argv=None):
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--angles", type=int, default=180)
     ap.add_argument("--target-iters", type=int, default=1000)
-    ap.add_argument("--oracle", action="store_true", help="also compare one warm-started solve with the FP64 oracle")
     ap.add_argument("--noise", type=float, default=0.01, help="Gaussian noise, fraction of each sinogram's max")
     ap.add_argument("--budgets", default="10,20,50,100,200", help="plain budgets K (r* = 1.01 r_plain(K))")
     ap.add_argument("--abs-targets", default="", help="absolute residual targets, e.g. 1e-3 (noise-free data)")
     ap.add_argument("--max-iters", type=int, default=600)
+    ap.add_argument("--constant-lr", action="store_true", help="no warm-up / cosine decay")
     ap.add_argument("--sparse-size", type=int, default=512)
     ap.add_argument("--sparse-angles", type=int, default=90)
     ap.add_argument("--out", default="")
@@ -237,7 +236,7 @@ def main(argv=None):
     log(f"dataset {args.train} x {args.size}^2 in {t_data:.1f} s")
     net = UNet(args.size, args.batch, seed=0)
     t0 = time.time()
-    hist = train(net, xs, ts, args.epochs, args.batch, args.lr, log=log)
+    hist = train(net, xs, ts, args.epochs, args.batch, args.lr, log=log, schedule=not args.constant_lr)
     torch.cuda.synchronize()
     t_train = time.time() - t0
     del xs, ts
@@ -247,9 +246,6 @@ def main(argv=None):
     res["eval_dense"] = evaluate(net, prob, args.eval, seed=777777, budgets=budgets, max_iters=args.max_iters,
                                  abs_targets=abs_t)
     log(json.dumps(res["eval_dense"]))
-    if args.oracle:
-        res["oracle_check"] = oracle_check(net, prob, seed=777777)
-        log(json.dumps(res["oracle_check"]))
     sparse = Problem(args.sparse_size, args.sparse_angles, noise=args.noise)
     net512 = UNet(args.sparse_size, 8, seed=0)
     net512.load(net.params())

@@ -49,7 +49,8 @@ def _conv_ref(x, w, b=None):
 
 
 @pytest.mark.parametrize("Bn,H,W,Cin,Cout", [(2, 16, 128, 32, 32), (1, 64, 64, 64, 128), (2, 32, 32, 96, 256),
-                                             (1, 128, 256, 32, 64)])
+                                             (1, 128, 256, 32, 64), (2, 8, 256, 96, 32), (1, 8, 128, 192, 64),
+                                             (1, 4, 128, 64, 96), (1, 4, 256, 128, 192), (1, 4, 128, 32, 256)])
 def test_conv3x3_forward_bias_relu(gpu, Bn, H, W, Cin, Cout):
     g = torch.Generator(device="cuda").manual_seed(Cin * Cout + H)
     x = _bf16(torch.randn(Bn, H, W, Cin, device="cuda", generator=g))
@@ -117,15 +118,54 @@ def test_conv3x3_weight_gradient(gpu, Bn, H, W, Cin, Cout, ksplit):
     y = _conv_ref(x.float(), wr)
     y.backward(dy.float())
     ref = wr.grad
-    dyT = dy.permute(3, 0, 1, 2).contiguous()                          # [Cout][B][H][W]
-    xc = x.permute(3, 0, 1, 2)                                         # [Cin][B][H][W]
-    xT3 = torch.zeros(3, Cin, Bn, H, W, dtype=torch.bfloat16, device="cuda")
-    xT3[0, ..., 1:] = xc[..., :-1]     # kx = 0: x[w - 1]
-    xT3[1] = xc
-    xT3[2, ..., :-1] = xc[..., 1:]     # kx = 2: x[w + 1]
+    cw = 64 if W >= 64 else 32
+
+    def blocked(t):   # [B][H][W][C] -> [B][H][W/cw][C][cw]
+        Bq, Hq, Wq, Cq = t.shape
+        return t.reshape(Bq, Hq, Wq // cw, cw, Cq).permute(0, 1, 2, 4, 3).contiguous()
+
+    dyT = blocked(dy)
+    xs = torch.zeros(3, Bn, H, W, Cin, dtype=torch.bfloat16, device="cuda")
+    xs[0, :, :, 1:] = x[:, :, :-1]     # kx = 0: x[w - 1]
+    xs[1] = x
+    xs[2, :, :, :-1] = x[:, :, 1:]     # kx = 2: x[w + 1]
+    xT3 = torch.stack([blocked(xs[k]) for k in range(3)])
     dw = torch.zeros(Cout, 9 * Cin, device="cuda")
     ctx = rt.context()
     rc = ctx.lib.synk_conv3x3_wgrad_bf16(ctx.handle, _p(dyT), _p(xT3), _p(dw), Cin, Cout, Bn, H, W, ksplit)
     ctx.check(rc, "wgrad")
     ctx.sync()
     assert _rel(dw, ref) < 1e-4
+
+
+@pytest.mark.parametrize("W,Cin,Cout,xoff,ldx", [(128, 64, 32, 32, 128), (256, 32, 96, 64, 96)])
+def test_conv3x3_row_strip_slices_and_backward_data(gpu, W, Cin, Cout, xoff, ldx):
+    """Rows of 128k pixels take the row-strip path: channel slices of a wider
+    input buffer, and the backward-data form with the ReLU mask."""
+    Bn, H = 1, 8
+    g = torch.Generator(device="cuda").manual_seed(W + Cin)
+    xbuf = _bf16(torch.relu(torch.randn(Bn, H, W, ldx, device="cuda", generator=g)))
+    x = xbuf[..., xoff:xoff + Cin]
+    w = _bf16(0.1 * torch.randn(Cout, 9 * Cin, device="cuda", generator=g))
+    bias = torch.randn(Cout, device="cuda", generator=g)
+    y = torch.zeros(Bn, H, W, Cout, dtype=torch.bfloat16, device="cuda")
+    ctx = rt.context()
+    rc = ctx.lib.synk_conv3x3_bf16(ctx.handle, _p(xbuf), ldx, xoff, Cin, Bn, H, W, _p(w), _p(bias), _p(y), Cout, 0,
+                                   Cout, 4, None, 0, 0)
+    ctx.check(rc, "conv")
+    ctx.sync()
+    assert _rel(y.float(), _conv_ref(x.float(), w.float(), bias)) < 1e-2
+    # backward data: dx = conv(dy, flipped transposed w) * (x > 0), written into a slice
+    dy = _bf16(torch.randn(Bn, H, W, Cout, device="cuda", generator=g))
+    xr = x.float().clone().requires_grad_(True)
+    _conv_ref(xr, w.float()).backward(dy.float())
+    ref = xr.grad * (x.float() > 0)
+    wt = _bf16(w.float().reshape(Cout, 9, Cin).flip(1).permute(2, 1, 0).reshape(Cin, 9 * Cout))
+    dxbuf = torch.zeros(Bn, H, W, ldx, dtype=torch.bfloat16, device="cuda")
+    rc = ctx.lib.synk_conv3x3_bf16(ctx.handle, _p(dy), Cout, 0, Cout, Bn, H, W, _p(wt), None, _p(dxbuf), ldx, xoff,
+                                   Cin, 2, _p(xbuf), ldx, xoff)
+    ctx.check(rc, "dgrad")
+    ctx.sync()
+    assert _rel(dxbuf[..., xoff:xoff + Cin].float(), ref) < 1e-2
+    rest = torch.cat([dxbuf[..., :xoff], dxbuf[..., xoff + Cin:]], dim=-1)
+    assert float(rest.float().abs().max()) == 0.0
