@@ -35,7 +35,7 @@ import numpy as np  # noqa: E402
 
 N_SIZE, N_ANGLES, N_DET = 2048, 2048, 2897     # the projector microbench's dense configuration
 METRIC = "SIRT ms to rel. residual 1e-3: warm-start vs plain, 1 GB300; FP/BP GB/s"
-LEGS = ("proj", "e2e", "sirt", "csr", "cpu")      # default legs; "batch", "stack", "sparse", "unet" on request
+LEGS = ("proj", "e2e", "sirt", "csr", "unet", "cpu")   # default legs; "batch", "stack", "sparse" on request
 
 
 def set_workload(size, angles, detectors):

@@ -90,18 +90,21 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     uint8_t *smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    // MODE_HALO: A = one 130-pixel row strip (128-byte rows), B = the 3 taps kx of the strip's ky
-    const uint32_t aBytes = MODE == MODE_HALO ? p.aStage : 128u * (uint32_t)p.kbytes;
-    const uint32_t bTap = (((uint32_t)p.N * (uint32_t)(MODE == MODE_HALO ? 128 : p.kbytes) + 1023u) / 1024u) * 1024u;
-    const uint32_t bBytes = MODE == MODE_HALO ? 3u * bTap : bTap;
+    // stage = A part + B part (sizes from the host; MODE_HALO: A = one 130-pixel
+    // row strip of 128-byte rows, B = the 3 taps kx of the strip's ky)
+    const uint32_t aBytes = p.aStage;
+    const uint32_t bBytes = p.bStage;
+    const uint32_t bTap = (uint32_t)p.N * 128u;        // MODE_HALO: one tap's weights
     const uint32_t stageBytes = aBytes + bBytes;
     const int S = p.stages;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stageBytes);
+    uint8_t *bres = smem + (size_t)S * stageBytes;      // resident B (MODE_HALO, p.bres > 0)
+    uint64_t *full = reinterpret_cast<uint64_t *>(bres + p.bres);
     uint64_t *empty = full + S;
     uint64_t *tfull = empty + S;
     uint64_t *tempty = tfull + 2;
     uint64_t *drain = tempty + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    uint64_t *bfull = drain + 1;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bfull + 1);
     float *sbias = reinterpret_cast<float *>(tmem_slot + 4);    // [gy * N] epilogue bias
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -119,6 +122,7 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
             mbar_init(&tempty[j], 4);
         }
         mbar_init(drain, 1);
+        mbar_init(bfull, 1);
         fence_mbar_init();
     }
     if (warp == 0 && lane == 0) {
@@ -138,6 +142,11 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
             // ---- TMA producer ----
             long long g = 0;   // chunks issued by this CTA
             bool fail = false;
+            if (MODE == MODE_HALO && p.bres) {
+                // all taps' weights once for the CTA's lifetime (one n tile)
+                mbar_arrive_expect_tx(bfull, p.bres);
+                tma_load_3d(bres, &tmB, bfull, 0, 0, 0);
+            }
             for (long long t = blockIdx.x; t < ntiles && !fail; t += gridDim.x) {
                 const TileInfo ti = tile_info<MODE>(p, t);
                 for (int kc = 0; kc < ti.nk; ++kc) {
@@ -158,11 +167,11 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
                         // chunk = (ky, channel chunk cc): the strip of row h0+ky-1,
                         // pixels w0-1 .. w0+128, and the weights of taps (ky, 0..2)
                         // (64-channel boxes; channels >= Cin are out of bounds and read as 0)
+                        // B: packed weights [chunk][tap][Cout][64]; the three taps of row ky
+                        // are one box (few large TMA operations keep the copy engine busy)
                         const int ky = kc / p.cchunks, cc = kc - ky * p.cchunks;
                         tma_load_4d(As, &tmA, &full[s], cc * 64, ti.w0 - 1, ti.h0 + ky - 1, ti.b);
-#pragma unroll
-                        for (int kx = 0; kx < 3; ++kx)
-                            tma_load_2d(Bs + kx * bTap, &tmB, &full[s], (ky * 3 + kx) * p.Cin + cc * 64, ti.n0);
+                        if (!p.bres) tma_load_3d(Bs, &tmB, &full[s], 0, ti.n0, cc * 9 + 3 * ky);
                     } else if (MODE == MODE_CONV) {
                         const int tap = kc / p.cchunks, cc = kc - tap * p.cchunks;
                         const int tky = tap / 3, tkx = tap - tky * 3;
@@ -178,8 +187,10 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
                         // blocked operands [image][row][pixel chunk][channel][pixel]: a box is
                         // one contiguous block; the tap's row shift is the H coordinate (zero
                         // outside the image) and its column shift the pre-shifted copy kx
-                        tma_load_5d(As, &tmA, &full[s], 0, ti.m0, wb, hb, bb);
-                        tma_load_5d(Bs, &tmB, &full[s], 0, ti.n0, wb, hb + ti.ky - 1, ti.kx * p.Bn + bb);
+                        // a stage holds kw x kh pixel chunks (one box per operand)
+                        tma_load_5d(As, &tmA, &full[s], 0, ti.m0, wb * p.kw, hb * p.kh, bb);
+                        tma_load_5d(Bs, &tmB, &full[s], 0, ti.n0, wb * p.kw, hb * p.kh + ti.ky - 1,
+                                    ti.kx * p.Bn + bb);
                     }
                     ++g;
                 }
@@ -188,6 +199,7 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
             // the last use of every stage (immediate on the normal path)
             const long long first = g > S ? g - S : 0;
             for (long long c = first; c < g; ++c) mbar_drain(&full[c % S], (uint32_t)(c / S) & 1u, p.limit_ns);
+            if (MODE == MODE_HALO && p.bres) mbar_drain(bfull, 0u, p.limit_ns);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -197,6 +209,7 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
             long long g = 0;
             int li = 0;
             bool fail = false;
+            if (MODE == MODE_HALO && p.bres && !mbar_wait(bfull, 0u, p.err, p.limit_ns)) fail = true;
             for (long long t = blockIdx.x; t < ntiles && !fail; t += gridDim.x, ++li) {
                 const TileInfo ti = tile_info<MODE>(p, t);
                 const int ab = li & 1;
@@ -216,13 +229,23 @@ __global__ void __launch_bounds__(192, 1) umma_kernel(const __grid_constant__ CU
                     if (MODE == MODE_HALO) {
                         // tap kx reads the strip from row kx (pixel w0+kx-1); only the
                         // chunk's valid channels (32 or 64) are multiplied
-                        const int cc = kc % p.cchunks;
+                        const int ky = kc / p.cchunks, cc = kc - ky * p.cchunks;
                         const uint32_t ksteps = (uint32_t)min(64, p.Cin - 64 * cc) / 16u;
+                        // weights of tap (ky, kx): resident block (cc*9 + 3ky + kx) or the stage's box kx
+                        const uint32_t bt0 = p.bres ? smem_u32(bres) + (uint32_t)(cc * 9 + 3 * ky) * bTap : b0;
                         for (uint32_t kx = 0; kx < 3u; ++kx)
                             for (uint32_t kk = 0; kk < ksteps; ++kk)
                                 mma_bf16(dt, smem_desc_sw128_at(a0 + kx * 128u + kk * 32u),
-                                         smem_desc(b0 + kx * bTap + kk * 32u, 128u), idesc,
+                                         smem_desc(bt0 + kx * bTap + kk * 32u, 128u), idesc,
                                          (kc | (int)kx | (int)kk) != 0 ? 1u : 0u);
+                    } else if (MODE == MODE_WGRAD) {
+                        // sub-chunk j of the stage: A rows at j*arows, B rows at j*N
+                        const uint32_t nsub = (uint32_t)(p.kw * p.kh);
+                        for (uint32_t j = 0; j < nsub; ++j)
+                            for (uint32_t kk = 0; kk < kbytes / 32u; ++kk)
+                                mma_bf16(dt, smem_desc(a0 + j * (uint32_t)p.arows * kbytes + kk * 32u, kbytes),
+                                         smem_desc(b0 + j * (uint32_t)p.N * kbytes + kk * 32u, kbytes), idesc,
+                                         (kc | (int)j | (int)kk) != 0 ? 1u : 0u);
                     } else {
                         for (uint32_t kk = 0; kk < kbytes / 32u; ++kk) {
                             mma_bf16(dt, smem_desc(a0 + kk * 32u, kbytes), smem_desc(b0 + kk * 32u, kbytes), idesc,
@@ -381,26 +404,26 @@ static int pow2_cols(int n) {
     return c;
 }
 
-static size_t stage_bytes(const GemmParams &p, bool halo) {
-    const size_t btap = ((size_t)p.N * (halo ? 128 : p.kbytes) + 1023) / 1024 * 1024;
-    return halo ? (size_t)p.aStage + 3 * btap : 128u * (size_t)p.kbytes + btap;
+static uint32_t kb_round(size_t b) { return (uint32_t)((b + 1023) / 1024 * 1024); }
+
+static size_t smem_bytes(const GemmParams &p, int gy) {
+    return 1024 + (size_t)p.stages * (p.aStage + p.bStage) + p.bres + 8 * (2 * p.stages + 6) + 16 +
+           4 * (size_t)gy * p.N;
 }
 
-static size_t smem_bytes(const GemmParams &p, int gy, bool halo) {
-    return 1024 + (size_t)p.stages * stage_bytes(p, halo) + 8 * (2 * p.stages + 5) + 16 + 4 * (size_t)gy * p.N;
-}
-
-static int pick_stages(int N, int kbytes) {
-    const size_t a = 128u * kbytes, b = ((size_t)N * kbytes + 1023) / 1024 * 1024;
-    int s = (int)((200 * 1024) / (a + b));
-    return s > 16 ? 16 : (s < 2 ? 2 : s);
+// stages of the given size in ~200 KB (the copy engine keeps few operations in
+// flight per SM, so more than a handful of stages buys nothing)
+static int pick_stages(uint32_t aStage, uint32_t bStage) {
+    int s = (int)((200 * 1024) / (aStage + bStage));
+    return s > 8 ? 8 : (s < 2 ? 2 : s);
 }
 
 // Persistent launch: min(tiles, SMs) CTAs (one per SM: ~200 KB of stages)
 // walk the gx x gy x gz tiles.
 template <int MODE, int EPI>
 static cudaError_t launch(const CUtensorMap &A, const CUtensorMap &B, GemmParams p, dim3 tiles, cudaStream_t st) {
-    const size_t smem = smem_bytes(p, (int)tiles.y, MODE == MODE_HALO);
+    const size_t smem = smem_bytes(p, (int)tiles.y);
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(umma_kernel<MODE, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
@@ -426,7 +449,9 @@ cudaError_t gemm_bf16(const uint16_t *A, const uint16_t *B, float *C, int M, int
     p.ncols = pow2_cols(N);
     p.kbytes = 128;
     p.nk = K / 64;
-    p.stages = pick_stages(N, 128);
+    p.aStage = 128u * 128u;
+    p.bStage = kb_round((size_t)N * 128);
+    p.stages = pick_stages(p.aStage, p.bStage);
     p.bytesA = 128u * 128u;
     p.bytesB = (uint32_t)N * 128u;
     p.out = C;
@@ -444,10 +469,28 @@ cudaError_t gemm_bf16(const uint16_t *A, const uint16_t *B, float *C, int M, int
     return launch<MODE_GEMM, EPI_F32>(ta, tb, p, dim3(M / 128, 1, 1), st);
 }
 
+// wp[(cc*9 + tap)*Cout + o][j] = w[o][tap*Cin + 64*cc + j] (0 past Cin): the
+// weights of the row-strip form, 64-channel chunks, taps and output channels
+// as rows of 128 bytes.
+__global__ void pack_weights_kernel(const uint16_t *__restrict__ w, uint16_t *__restrict__ wp, int Cin, int Cout,
+                                    int cchunks) {
+    const long long n = (long long)cchunks * 9 * Cout * 64;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(i & 63);
+        const long long r = i >> 6;
+        const int o = (int)(r % Cout);
+        const int t = (int)(r / Cout);          // cc*9 + tap
+        const int cc = t / 9, tap = t - cc * 9;
+        const int c = 64 * cc + j;
+        wp[i] = c < Cin ? w[(long long)o * 9 * Cin + tap * Cin + c] : (uint16_t)0;
+    }
+}
+
 // Image rows of 128k pixels: a tile is 128 pixels of one row, and per input
 // row ky and 64-channel chunk ONE strip of 130 pixels (halo of one on each
-// side) is loaded; the three taps kx are views of it shifted by kx rows.
-// Compared with a box per tap this moves a third of the input through TMA.
+// side) is loaded, with the three taps' weights as one more box; the taps kx
+// are views of the strip shifted by kx rows.  Compared with a box per tap
+// this issues a third of the copy operations and moves a third of the input.
 static cudaError_t conv3x3_halo(const ConvArgs &c, int epi, int ntile, int *err, unsigned long long limit_ns,
                                 cudaStream_t st) {
     GemmParams p = {};
@@ -456,19 +499,26 @@ static cudaError_t conv3x3_halo(const ConvArgs &c, int epi, int ntile, int *err,
     p.kbytes = 128;
     p.cchunks = (c.Cin + 63) / 64;
     p.nk = 3 * p.cchunks;
-    p.aStage = (130u * 128u + 1023u) / 1024u * 1024u;
+    p.aStage = kb_round(130u * 128u);
+    // weights resident when one n tile covers Cout and they leave room for 4 strips
+    const size_t bfull_bytes = (size_t)p.cchunks * 9 * ntile * 128;
+    const bool resident = ntile == c.Cout && bfull_bytes + 4 * (size_t)p.aStage <= 200u * 1024u;
+    if (resident) {
+        p.bres = (uint32_t)bfull_bytes;
+        p.bStage = 0;
+        const int s = (int)((200u * 1024u - bfull_bytes) / p.aStage);
+        p.stages = s > 8 ? 8 : s;
+    } else {
+        p.bStage = kb_round(3u * (size_t)ntile * 128u);
+        p.stages = pick_stages(p.aStage, p.bStage);
+    }
     p.H = c.H;
     p.W = c.W;
     p.Cin = c.Cin;
     p.bw = 128;
     p.bh = 1;
     p.bytesA = 130u * 128u;
-    p.bytesB = 3u * (uint32_t)ntile * 128u;
-    {
-        const size_t st1 = stage_bytes(p, true);
-        int s = (int)((200 * 1024) / st1);
-        p.stages = s > 16 ? 16 : (s < 2 ? 2 : s);
-    }
+    p.bytesB = resident ? 0u : 3u * (uint32_t)ntile * 128u;
     p.out = c.y;
     p.ldo = c.ldy;
     p.coff = c.yoff;
@@ -478,22 +528,36 @@ static cudaError_t conv3x3_halo(const ConvArgs &c, int epi, int ntile, int *err,
     p.moff = c.moff;
     p.err = err;
     p.limit_ns = limit_ns;
+    // packed weights in stream-ordered scratch
+    const long long npk = (long long)p.cchunks * 9 * c.Cout * 64;
+    uint16_t *wp = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&wp), (size_t)npk * 2, st);
+    if (e != cudaSuccess) return e;
+    pack_weights_kernel<<<(unsigned)((npk + 255) / 256 < 1024 ? (npk + 255) / 256 : 1024), 256, 0, st>>>(
+        c.w, wp, c.Cin, c.Cout, p.cchunks);
+    if ((e = cudaGetLastError()) != cudaSuccess) {
+        cudaFreeAsync(wp, st);
+        return e;
+    }
     CUtensorMap ta, tb;
     const uint64_t da[4] = {(uint64_t)c.Cin, (uint64_t)c.W, (uint64_t)c.H, (uint64_t)c.B};
     const uint64_t sa[3] = {(uint64_t)c.ldx * 2, (uint64_t)c.ldx * 2 * c.W, (uint64_t)c.ldx * 2 * c.W * c.H};
     const uint32_t ba[4] = {64, 130, 1, 1};
-    const uint64_t db[2] = {(uint64_t)9 * c.Cin, (uint64_t)c.Cout}, sb[1] = {(uint64_t)9 * c.Cin * 2};
-    const uint32_t bbx[2] = {64, (uint32_t)ntile};
-    cudaError_t e;
-    if ((e = tensor_map(&ta, c.x + c.xoff, 4, da, sa, ba, 128)) != cudaSuccess) return e;
-    if ((e = tensor_map(&tb, c.w, 2, db, sb, bbx, 128)) != cudaSuccess) return e;
+    const uint64_t db[3] = {64, (uint64_t)c.Cout, (uint64_t)p.cchunks * 9};
+    const uint64_t sb[2] = {128, (uint64_t)c.Cout * 128};
+    const uint32_t bbx[3] = {64, (uint32_t)ntile, resident ? (uint32_t)(p.cchunks * 9) : 3u};
     const dim3 grid((unsigned)((long long)c.B * c.H * c.W / 128), (unsigned)(c.Cout / ntile), 1);
-    switch (epi) {
-        case EPI_BIAS_RELU: return launch<MODE_HALO, EPI_BIAS_RELU>(ta, tb, p, grid, st);
-        case EPI_BIAS: return launch<MODE_HALO, EPI_BIAS>(ta, tb, p, grid, st);
-        case EPI_MASK: return launch<MODE_HALO, EPI_MASK>(ta, tb, p, grid, st);
-        default: return cudaErrorInvalidValue;
+    if ((e = tensor_map(&ta, c.x + c.xoff, 4, da, sa, ba, 128)) == cudaSuccess &&
+        (e = tensor_map(&tb, wp, 3, db, sb, bbx, 128)) == cudaSuccess) {
+        switch (epi) {
+            case EPI_BIAS_RELU: e = launch<MODE_HALO, EPI_BIAS_RELU>(ta, tb, p, grid, st); break;
+            case EPI_BIAS: e = launch<MODE_HALO, EPI_BIAS>(ta, tb, p, grid, st); break;
+            case EPI_MASK: e = launch<MODE_HALO, EPI_MASK>(ta, tb, p, grid, st); break;
+            default: e = cudaErrorInvalidValue;
+        }
     }
+    const cudaError_t e2 = cudaFreeAsync(wp, st);
+    return e != cudaSuccess ? e : e2;
 }
 
 cudaError_t conv3x3(const ConvArgs &c, int epi, int *err, unsigned long long limit_ns, cudaStream_t st) {
@@ -504,7 +568,7 @@ cudaError_t conv3x3(const ConvArgs &c, int epi, int *err, unsigned long long lim
     const int ntile = c.Cout <= 256 ? c.Cout : (c.Cout % 192 == 0 ? 192 : (c.Cout % 128 == 0 ? 128 : 0));
     if (ntile == 0) return cudaErrorInvalidValue;
     // the row-strip form when a tile is one image row and two stages fit
-    if (c.W % 128 == 0 && 17408 + 3 * ((ntile * 128 + 1023) / 1024 * 1024) <= 100 * 1024)
+    if (c.W % 128 == 0 && kb_round(130u * 128u) + kb_round(3u * (size_t)ntile * 128u) <= 100u * 1024u)
         return conv3x3_halo(c, epi, ntile, err, limit_ns, st);
     const int bw = c.W >= 128 ? 128 : c.W;
     const int bh = 128 / bw;
@@ -519,7 +583,9 @@ cudaError_t conv3x3(const ConvArgs &c, int epi, int *err, unsigned long long lim
     p.kbytes = kb;
     p.cchunks = c.Cin / cw;
     p.nk = 9 * p.cchunks;
-    p.stages = pick_stages(ntile, kb);
+    p.aStage = 128u * (uint32_t)kb;
+    p.bStage = kb_round((size_t)ntile * kb);
+    p.stages = pick_stages(p.aStage, p.bStage);
     p.H = c.H;
     p.W = c.W;
     p.Cin = c.Cin;
@@ -565,36 +631,58 @@ cudaError_t conv3x3_wgrad(const WgradArgs &w, int *err, unsigned long long limit
     const int kbytes = bwk * 2;
     const int ntile = w.Cin <= 256 ? w.Cin : (w.Cin % 192 == 0 ? 192 : 128);
     if (w.Cin % ntile) return cudaErrorInvalidValue;
+    // a stage holds a super-chunk of kw x kh pixel chunks (4 where the image
+    // allows): one TMA box per operand per stage
+    const int nwb = w.W / bwk;
+    const int arows = w.Cout < 128 ? w.Cout : 128;
+    int kw = 1, kh = 1;
+    for (int nsub = 4; nsub >= 1; nsub /= 2) {      // the largest that leaves room for two stages
+        const int tw = nwb >= nsub ? nsub : nwb;
+        const int th = nsub / tw;
+        if (nwb % tw || w.H % th) continue;
+        const size_t stage = kb_round(((size_t)(nsub - 1) * arows + 128) * kbytes) +
+                             kb_round((size_t)nsub * ntile * kbytes);
+        if (2 * stage <= 200u * 1024u) {
+            kw = tw;
+            kh = th;
+            break;
+        }
+    }
     GemmParams p = {};
     p.N = ntile;
     p.ncols = pow2_cols(ntile);
     p.kbytes = kbytes;
-    p.stages = pick_stages(ntile, kbytes);
+    p.kw = kw;
+    p.kh = kh;
+    p.arows = arows;
+    // the M = 128 MMA of the last sub-chunk reads 128 rows from its start
+    p.aStage = kb_round(((size_t)(kw * kh - 1) * arows + 128) * kbytes);
+    p.bStage = kb_round((size_t)kw * kh * ntile * kbytes);
+    p.stages = pick_stages(p.aStage, p.bStage);
     p.Cin = w.Cin;
     p.bwk = bwk;
     p.bhk = bhk;
-    p.nb_w = w.W / bwk;
-    p.nb_h = w.H / bhk;
+    p.nb_w = nwb / kw;
+    p.nb_h = w.H / kh;
     p.Bn = w.B;
     p.ksplit = w.ksplit;
     p.mvalid = w.Cout;
-    const int arows = w.Cout < 128 ? w.Cout : 128;
-    p.bytesA = (uint32_t)arows * (uint32_t)kbytes;
-    p.bytesB = (uint32_t)ntile * (uint32_t)kbytes;
+    p.bytesA = (uint32_t)(kw * kh * arows * kbytes);
+    p.bytesB = (uint32_t)(kw * kh * ntile * kbytes);
     p.out = w.dw;
     p.ldo = 9LL * w.Cin;
     p.err = err;
     p.limit_ns = limit_ns;
     CUtensorMap ta, tb;
-    const uint64_t nwb = (uint64_t)(w.W / bwk);
-    const uint64_t da[5] = {(uint64_t)bwk, (uint64_t)w.Cout, nwb, (uint64_t)w.H, (uint64_t)w.B};
-    const uint64_t sa[4] = {(uint64_t)bwk * 2, (uint64_t)w.Cout * bwk * 2, nwb * w.Cout * bwk * 2,
-                            (uint64_t)w.H * nwb * w.Cout * bwk * 2};
-    const uint32_t ba[5] = {(uint32_t)bwk, (uint32_t)arows, 1, 1, 1};
-    const uint64_t db[5] = {(uint64_t)bwk, (uint64_t)w.Cin, nwb, (uint64_t)w.H, (uint64_t)3 * w.B};
-    const uint64_t sb[4] = {(uint64_t)bwk * 2, (uint64_t)w.Cin * bwk * 2, nwb * w.Cin * bwk * 2,
-                            (uint64_t)w.H * nwb * w.Cin * bwk * 2};
-    const uint32_t bbx[5] = {(uint32_t)bwk, (uint32_t)ntile, 1, 1, 1};
+    const uint64_t nwbu = (uint64_t)nwb;
+    const uint64_t da[5] = {(uint64_t)bwk, (uint64_t)w.Cout, nwbu, (uint64_t)w.H, (uint64_t)w.B};
+    const uint64_t sa[4] = {(uint64_t)bwk * 2, (uint64_t)w.Cout * bwk * 2, nwbu * w.Cout * bwk * 2,
+                            (uint64_t)w.H * nwbu * w.Cout * bwk * 2};
+    const uint32_t ba[5] = {(uint32_t)bwk, (uint32_t)arows, (uint32_t)kw, (uint32_t)kh, 1};
+    const uint64_t db[5] = {(uint64_t)bwk, (uint64_t)w.Cin, nwbu, (uint64_t)w.H, (uint64_t)3 * w.B};
+    const uint64_t sb[4] = {(uint64_t)bwk * 2, (uint64_t)w.Cin * bwk * 2, nwbu * w.Cin * bwk * 2,
+                            (uint64_t)w.H * nwbu * w.Cin * bwk * 2};
+    const uint32_t bbx[5] = {(uint32_t)bwk, (uint32_t)ntile, (uint32_t)kw, (uint32_t)kh, 1};
     cudaError_t e;
     if ((e = tensor_map(&ta, w.dyT, 5, da, sa, ba, kbytes)) != cudaSuccess) return e;
     if ((e = tensor_map(&tb, w.xT3, 5, db, sb, bbx, kbytes)) != cudaSuccess) return e;

@@ -15,11 +15,12 @@ struct GemmParams {
     int gx, gy, gz;       // tile grid (x fastest); set by the launcher
     long long ntiles;
     uint32_t bytesA, bytesB;
+    uint32_t aStage, bStage;   // bytes of the A and B parts of a stage (1 KB multiples)
+    uint32_t bres;             // MODE_HALO: bytes of the B operand held resident (0: streamed per chunk)
     // MODE_CONV / MODE_HALO
     int H, W, Cin, bw, bh, cchunks;
-    uint32_t aStage;      // MODE_HALO: bytes of the A strip in a stage (130 rows x 128 B, 1 KB aligned)
-    // MODE_WGRAD
-    int bwk, bhk, nb_w, nb_h, Bn, ksplit, mvalid;
+    // MODE_WGRAD: K super-chunks of kw x kh pixel chunks (bwk pixels each) per stage
+    int bwk, bhk, nb_w, nb_h, Bn, ksplit, mvalid, kw, kh, arows;
     // epilogue
     void *out;
     long long ldo;
