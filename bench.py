@@ -129,6 +129,24 @@ def cpu_reference_rate(budget_s=12.0, seed=0):
             "cores": cores}
 
 
+def cpu_sirt_cfg0(iterations=200):
+    """Plain SIRT on the N=128 configuration (128 angles, 182 detectors, 1 %
+    noise, 200 iterations) by the CPU port on all host cores: seconds for the
+    full run (the reference's own CPU-runnable case, timed whole)."""
+    from oracle import cpu_ref
+
+    from synkrotomo_gb300 import phantom
+    cores = host_cores()
+    cpu_ref.set_threads(cores)
+    g = phantom.geometry(128, 128)
+    img = phantom.ellipse_phantom(128, 0)
+    b = phantom.add_noise(cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, img), 0, 0.01)
+    x0 = np.zeros(128 * 128, np.float32)
+    t0 = time.perf_counter()
+    cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, x0, b, iterations)
+    return {"s": time.perf_counter() - t0, "iterations": iterations, "cores": cores}
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -147,11 +165,17 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu_index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # nvidia-smi takes a moment to start: wait for its first sample so
+            # that the samples taken inside the timed region are its own
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self.start = len(self.lines)
         return self
 
     def _read(self):
@@ -170,7 +194,9 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        # the samples taken during the region (else the last one before its end)
+        inside = self.lines[self.start:] or self.lines[-1:]
+        for line in inside:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -657,6 +683,10 @@ def main():
         u["bf16_peak_tflops"] = bf16
         line["unet_cfg4"] = u
     if "cpu" in args.legs:
+        if "sirt_cfg0" in line:
+            c0 = cpu_sirt_cfg0()
+            line["sirt_cfg0"]["cpu_port_200_iterations_ms"] = c0["s"] * 1e3
+            line["sirt_cfg0"]["cpu_port_cores"] = c0["cores"]
         r = cpu_reference_rate(budget_s=10.0)
         cv = step_bytes() / r["step_s"] / 1e9
         line["cpu_baseline"] = {"value": cv, "unit": "GB/s", "cores": r["cores"], "kind": "port",
