@@ -63,15 +63,36 @@ int cuda_fail(synk_context *ctx, cudaError_t e, const char *what) {
 
 // Stream-ordered scratch memory, released on the same stream when it goes out
 // of scope (the frees are ordered after every kernel enqueued before them).
+// reserve() takes one block that later get() calls carve (256-byte aligned),
+// so a call with several small buffers costs one allocation and one free.
 struct Scratch {
     cudaStream_t st;
     std::vector<void *> ptrs;
+    char *arena = nullptr;
+    size_t arena_left = 0;
     explicit Scratch(cudaStream_t s) : st(s) {}
     ~Scratch() {
         for (void *p : ptrs) cudaFreeAsync(p, st);
     }
+    static size_t round(size_t b) { return (b + 16 + 255) / 256 * 256; }
+    cudaError_t reserve(size_t bytes) {
+        void *p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, bytes, st);
+        if (e != cudaSuccess) return e;
+        ptrs.push_back(p);
+        arena = static_cast<char *>(p);
+        arena_left = bytes;
+        return cudaSuccess;
+    }
     template <class T>
     cudaError_t get(T **out, size_t count) {
+        const size_t need = round(count * sizeof(T));
+        if (need <= arena_left) {
+            *out = reinterpret_cast<T *>(arena);
+            arena += need;
+            arena_left -= need;
+            return cudaSuccess;
+        }
         void *p = nullptr;
         cudaError_t e = cudaMallocAsync(&p, count * sizeof(T) + 16, st);
         if (e != cudaSuccess) return e;
@@ -80,6 +101,12 @@ struct Scratch {
         return cudaSuccess;
     }
 };
+
+// scratch bytes of the angle lists (make_lists)
+size_t lists_bytes(int64_t a) {
+    return Scratch::round(sizeof(int) * ((size_t)a + 64)) + Scratch::round(sizeof(int) * (size_t)a) +
+           Scratch::round(sizeof(int) * 4);
+}
 
 int64_t isqrt64(int64_t n) {
     if (n < 0) return -1;
@@ -176,6 +203,10 @@ int forward(synk_context *ctx, float *out, const float *angles, int64_t a, float
     Scratch sc(st);
     AngleGeom *geom;
     float *xpad, *xTpad;
+    const size_t npad = (size_t)size * (size + 2);
+    SYNK_CUDA(sc.reserve(Scratch::round(sizeof(AngleGeom) * (size_t)a) + 2 * Scratch::round(sizeof(float) * npad) +
+                         lists_bytes(a)),
+              "cudaMallocAsync(scratch)");
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
     SYNK_CUDA(sc.get(&xpad, (size_t)size * (size + 2)), "cudaMallocAsync(padded image)");
     SYNK_CUDA(sc.get(&xTpad, (size_t)size * (size + 2)), "cudaMallocAsync(padded transposed image)");
@@ -201,6 +232,9 @@ int backward(synk_context *ctx, float *out, const float *angles, int64_t a, floa
     cudaStream_t st = ctx->stream;
     Scratch sc(st);
     AngleGeom *geom;
+    SYNK_CUDA(sc.reserve(Scratch::round(sizeof(AngleGeom) * (size_t)a) + Scratch::round(sizeof(float) * (size_t)p) +
+                         lists_bytes(a)),
+              "cudaMallocAsync(scratch)");
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
     SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size_in, geom);

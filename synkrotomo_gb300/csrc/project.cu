@@ -16,6 +16,18 @@
 
 namespace synk {
 
+int device_sms() {
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cache[dev]) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) return 152;
+        cache[dev] = sms;
+    }
+    return cache[dev];
+}
+
 // sirtlib.fut:28-44 per angle, plus the constants of both traversals.  cos
 // and sin are evaluated in FP64 and rounded once, so they are the correctly
 // rounded float32 values that the reference's f32.cos / f32.sin return for
@@ -115,8 +127,9 @@ cudaError_t launch_angle_lists(const ProbGeom &P, int *order, int *exact, int *c
     return cudaGetLastError();
 }
 
-// xpad[z][r][c+1] = x[z][r][c], xTpad[z][c][r+1] = x[z][r][c] (row stride N+2;
-// the pad columns are zeroed by the caller).
+// xpad[z][r][c+1] = x[z][r][c], xTpad[z][c][r+1] = x[z][r][c] (row stride N+2);
+// the blocks of the first and last tile column (row) also write the zero pad
+// columns 0 and N+1 of their rows of xpad (xTpad).
 __global__ void pad_kernel(const float *__restrict__ x, float *__restrict__ xpad, float *__restrict__ xTpad, int N) {
     __shared__ float tile[32][33];
     const size_t off = (size_t)blockIdx.z * N * N;
@@ -130,6 +143,20 @@ __global__ void pad_kernel(const float *__restrict__ x, float *__restrict__ xpad
             xpad[offp + (size_t)r * (N + 2) + c + 1] = v;
         }
     }
+    if (threadIdx.y == 0 && (blockIdx.x == 0 || blockIdx.x == gridDim.x - 1)) {
+        const int r = by + threadIdx.x;
+        if (r < N) {
+            if (blockIdx.x == 0) xpad[offp + (size_t)r * (N + 2)] = 0.0f;
+            if (blockIdx.x == gridDim.x - 1) xpad[offp + (size_t)r * (N + 2) + N + 1] = 0.0f;
+        }
+    }
+    if (threadIdx.y == 1 && (blockIdx.y == 0 || blockIdx.y == gridDim.y - 1)) {
+        const int c = bx + threadIdx.x;
+        if (c < N) {
+            if (blockIdx.y == 0) xTpad[offp + (size_t)c * (N + 2)] = 0.0f;
+            if (blockIdx.y == gridDim.y - 1) xTpad[offp + (size_t)c * (N + 2) + N + 1] = 0.0f;
+        }
+    }
     __syncthreads();
     for (int y = threadIdx.y; y < 32; y += 8) {
         const int c = bx + y, r = by + threadIdx.x;
@@ -138,10 +165,6 @@ __global__ void pad_kernel(const float *__restrict__ x, float *__restrict__ xpad
 }
 
 cudaError_t launch_pad(const float *x, float *xpad, float *xTpad, int N, int nslices, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(xpad, 0, sizeof(float) * (size_t)nslices * N * (N + 2), stream);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(xTpad, 0, sizeof(float) * (size_t)nslices * N * (N + 2), stream);
-    if (e != cudaSuccess) return e;
     dim3 grid((N + 31) / 32, (N + 31) / 32, nslices);
     pad_kernel<<<grid, dim3(32, 8), 0, stream>>>(x, xpad, xTpad, N);
     return cudaGetLastError();
@@ -213,8 +236,7 @@ __global__ void __launch_bounds__(256) fp_exact_kernel(ProbGeom P, AngleLists L,
 
 // Rows split S ways when the rays alone give too few warps to fill the GPU.
 static int fp_row_split(long long warps) {
-    int sms = 152, dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int sms = device_sms();
     const long long want = (long long)sms * 48;
     int S = 1;
     while (S < 8 && warps * S < want) S *= 2;

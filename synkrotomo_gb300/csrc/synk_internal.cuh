@@ -300,6 +300,9 @@ __device__ __forceinline__ AngleGeom load_geom(const AngleGeom *__restrict__ gt,
 // Kernel launchers implemented in the .cu files (all enqueue on `stream`).
 // ---------------------------------------------------------------------------
 struct AngleLists;
+// SM count of the current device, queried once per device
+int device_sms();
+
 cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStream_t stream);
 cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad, const float *xTpad, float *sino,
                       cudaStream_t stream);

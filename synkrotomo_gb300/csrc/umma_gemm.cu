@@ -427,9 +427,7 @@ static cudaError_t launch(const CUtensorMap &A, const CUtensorMap &B, GemmParams
     cudaError_t e = cudaFuncSetAttribute(umma_kernel<MODE, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int sms = device_sms();
     p.gx = (int)tiles.x;
     p.gy = (int)tiles.y;
     p.gz = (int)tiles.z;

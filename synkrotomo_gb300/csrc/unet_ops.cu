@@ -316,46 +316,51 @@ __global__ void __launch_bounds__(256) head_bwd_kernel(const float *__restrict__
 // image row (cw = 64 when W >= 64, else 32), each chunk stored as [C][cw].
 // shifted = 0: out[q][c][j] = in[q*cw + j][c] (one copy); shifted = 1: three
 // copies, copy k at k*P*C, holding in[p + k - 1][c] when pixel p+k-1 is in
-// p's image row (w+k-1 in [0, W)), else 0.  A block transposes 64 pixels x 64
-// channels through shared memory (plus one halo pixel on each side), reading
-// 16-byte vectors and writing pixel pairs; the writes of a chunk are contiguous.
+// p's image row (w+k-1 in [0, W)), else 0.  A block handles 128 pixels (plus
+// one halo pixel on each side) x 64 channels: 16-byte loads into a
+// channel-major shared tile, then 16-byte stores of 8 consecutive pixels of
+// one channel, so each warp writes whole 128-byte lines.
 __global__ void __launch_bounds__(256) to_cmajor_kernel(const uint16_t *__restrict__ in, int ldi, int ioff,
                                                         uint16_t *__restrict__ out, int C, long long P, int W,
                                                         int shifted) {
-    __shared__ __align__(16) uint16_t tile[66][72];   // [pixel p0-1 .. p0+64][channel], rows padded
-    const long long p0 = (long long)blockIdx.x * 64;
+    __shared__ uint16_t tile[64][130];   // [channel][pixel p0-1 .. p0+128]; 65-word rows
+    const long long p0 = (long long)blockIdx.x * 128;
     const int c0 = blockIdx.y * 64;
+    const int cn = min(64, C - c0);      // multiple of 8
+    const int G = cn / 8;
     const int cw = W >= 64 ? 64 : 32;
-    const int cn = min(64, C - c0);     // multiple of 8
-    for (int i = threadIdx.x; i < 66 * 8; i += blockDim.x) {
-        const int r = i >> 3, g = i & 7;
+    for (int i = threadIdx.x; i < 130 * G; i += blockDim.x) {
+        const int r = i / G, h = i - r * G;
         const long long p = p0 - 1 + r;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (8 * g < cn && p >= 0 && p < P) v = ld8(in + p * ldi + ioff + c0 + 8 * g);
-        *reinterpret_cast<uint4 *>(&tile[r][8 * g]) = v;
+        if (p >= 0 && p < P) v = ld8(in + p * ldi + ioff + c0 + 8 * h);
+        const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) tile[8 * h + k][r] = (uint16_t)((k & 1) ? (wv[k >> 1] >> 16) : (wv[k >> 1] & 0xffffu));
     }
     __syncthreads();
     const int ncopies = shifted ? 3 : 1;
-    // thread = (channel, pixel pair); 32 pairs per channel
-    for (int i = threadIdx.x; i < cn * 32; i += blockDim.x) {
-        const int c = i >> 5, pr = (i & 31) * 2;
-        const long long p = p0 + pr;       // even; p and p+1 share a chunk (cw even)
-        if (p >= P) continue;
-        const int w0 = (int)(p % W);
-        const int wp[2] = {w0, w0 + 1 == W ? 0 : w0 + 1};
+    // thread = (channel c, group g of 8 pixels); groups fastest
+    for (int i = threadIdx.x; i < 16 * cn; i += blockDim.x) {
+        const int g = i & 15, c = i >> 4;
+        const long long p = p0 + 8 * g;
+        if (p >= P) continue;            // P is a multiple of 8: a group is wholly in or out
+        const int w0 = (int)(p % W);     // the group lies in one image row (W multiple of 8)
         const long long q = p / cw;
         const int j = (int)(p - q * cw);
         for (int k = 0; k < ncopies; ++k) {
             const int dsh = shifted ? k - 1 : 0;
-            uint16_t v[2];
+            uint32_t wv[4];
 #pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int w = wp[e];
-                const bool in_row = w + dsh >= 0 && w + dsh < W;
-                v[e] = in_row ? tile[pr + e + 1 + dsh][c] : (uint16_t)0;
+            for (int e = 0; e < 8; e += 2) {
+                const bool in0 = w0 + e + dsh >= 0 && w0 + e + dsh < W;
+                const bool in1 = w0 + e + 1 + dsh >= 0 && w0 + e + 1 + dsh < W;
+                const uint32_t v0 = in0 ? tile[c][8 * g + e + 1 + dsh] : 0u;
+                const uint32_t v1 = in1 ? tile[c][8 * g + e + 2 + dsh] : 0u;
+                wv[e >> 1] = v0 | (v1 << 16);
             }
             uint16_t *o = out + (long long)k * P * C + (q * C + c0 + c) * cw + j;
-            *reinterpret_cast<uint32_t *>(o) = (uint32_t)v[0] | ((uint32_t)v[1] << 16);
+            *reinterpret_cast<uint4 *>(o) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
         }
     }
 }
@@ -492,7 +497,7 @@ cudaError_t to_cmajor(const uint16_t *in, int ldi, int ioff, uint16_t *out, int 
                       cudaStream_t st) {
     if (!v8(C) || !v8(ldi) || !v8(ioff) || W < 32 || W % (W >= 64 ? 64 : 32) || P % W)
         return cudaErrorInvalidValue;
-    dim3 grid((unsigned)((P + 63) / 64), (unsigned)((C + 63) / 64));
+    dim3 grid((unsigned)((P + 127) / 128), (unsigned)((C + 63) / 64));
     to_cmajor_kernel<<<grid, 256, 0, st>>>(in, ldi, ioff, out, C, P, W, shifted);
     return cudaGetLastError();
 }
