@@ -141,7 +141,7 @@ def first_below(hist: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
 
 
 def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 100, 200), max_iters: int = 600,
-             abs_targets=()):
+             abs_targets=(), per_image_count: int = 16):
     """Plain zero-start SIRT vs warm-started SIRT on n held-out images.
 
     For each plain budget K: r*_i = 1.01 x the residual plain SIRT reaches on
@@ -151,7 +151,9 @@ def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 1
     an image that never reaches r*_i counts max_iters and is reported).
     Milliseconds are measured on batched runs that stop each image at its own
     r*_i when r* is absolute, and at the loosest r* of the batch otherwise; the
-    warm run includes the normalised backprojection and the network."""
+    warm run includes the normalised backprojection and the network.  Also,
+    for the first per_image_count images solved one launch each to their own
+    r*_i, the summed milliseconds (the cost a single-image caller sees)."""
     plain_len = max(max(budgets) if budgets else 0, max_iters if abs_targets else 0)
     imgs = ellipse_batch(n, prob.size, seed)
     b = prob.sinograms(imgs, seed)
@@ -178,10 +180,33 @@ def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 1
             ms[label] = t0.elapsed_time(t1)
         return ms
 
+    def per_image(rstar, count):
+        """Summed ms of `count` images solved one launch each to their own r*
+        (warm: one SIRT update, the network and the warm-started solve)."""
+        ms = {"plain": 0.0, "warm": 0.0}
+        for i in range(count):
+            bi = b[i:i + 1]
+            tol_i = float(rstar[i].item())
+            for label in ("plain", "warm"):
+                for rep in range(2):                   # first run warms up
+                    torch.cuda.synchronize()
+                    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    t0.record()
+                    start = None
+                    if label == "warm" and not bool(fallback[i]):
+                        xa, _, _ = prob.sirt(bi, 1)
+                        start = net.forward(xa.view(1, prob.size, prob.size)).view(1, -1)
+                    prob.sirt(bi, max_iters, start=start, tol=tol_i)
+                    t1.record()
+                    torch.cuda.synchronize()
+                ms[label] += t0.elapsed_time(t1)
+        return ms
+
     def row(rstar, tol):
         it_plain = first_below(hp, rstar).float()
         it_warm = torch.where(fallback, it_plain, first_below(hw, rstar).float())
         ms = timed(tol)
+        pim = per_image(rstar, min(per_image_count, n))
         return {"target_residual_mean": float(rstar.mean().item()),
                 "plain_iterations_mean": float(it_plain.mean().item()),
                 "warm_iterations_mean": float(it_warm.mean().item()),
@@ -191,7 +216,10 @@ def evaluate(net: UNet, prob: Problem, n: int, seed: int, budgets=(10, 20, 50, 1
                 "warm_not_reached": int((it_warm >= hw.shape[1]).sum().item()),
                 "speedup_iterations": float(it_plain.mean().item() / max(it_warm.mean().item(), 1e-9)),
                 "batched_ms_plain": ms["plain"], "batched_ms_warm": ms["warm"],
-                "speedup_ms": ms["plain"] / max(ms["warm"], 1e-9)}
+                "speedup_ms": ms["plain"] / max(ms["warm"], 1e-9),
+                "per_image_images": min(per_image_count, n),
+                "per_image_ms_plain": pim["plain"], "per_image_ms_warm": pim["warm"],
+                "speedup_per_image_ms": pim["plain"] / max(pim["warm"], 1e-9)}
 
     rows = []
     for Kb in budgets:
