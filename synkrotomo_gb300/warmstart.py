@@ -248,6 +248,9 @@ def main(argv=None):
     ap.add_argument("--abs-targets", default="", help="absolute residual targets, e.g. 1e-3 (noise-free data)")
     ap.add_argument("--max-iters", type=int, default=600)
     ap.add_argument("--constant-lr", action="store_true", help="no warm-up / cosine decay")
+    ap.add_argument("--mix-angles", type=int, default=0,
+                    help="also train on this angle count (half the phantoms each) for the sparse-view case")
+    ap.add_argument("--skip-sparse", action="store_true", help="no sparse-view evaluation")
     ap.add_argument("--sparse-size", type=int, default=512)
     ap.add_argument("--sparse-angles", type=int, default=90)
     ap.add_argument("--out", default="")
@@ -258,7 +261,17 @@ def main(argv=None):
     abs_t = tuple(float(v) for v in args.abs_targets.split(",") if v)
     prob = Problem(args.size, args.angles, noise=args.noise)
     t0 = time.time()
-    xs, ts = make_dataset(prob, args.train, seed=1, target_iters=args.target_iters)
+    if args.mix_angles:
+        # half the pairs at the evaluation geometry, half at the extra angle count
+        # (same image size, so one network sees both streak patterns)
+        half = args.train // 2
+        xa, ta = make_dataset(prob, half, seed=1, target_iters=args.target_iters)
+        pmix = Problem(args.size, args.mix_angles, noise=args.noise)
+        xb, tb = make_dataset(pmix, args.train - half, seed=2, target_iters=args.target_iters)
+        xs, ts = torch.cat([xa, xb]), torch.cat([ta, tb])
+        del xa, ta, xb, tb
+    else:
+        xs, ts = make_dataset(prob, args.train, seed=1, target_iters=args.target_iters)
     torch.cuda.synchronize()
     t_data = time.time() - t0
     log(f"dataset {args.train} x {args.size}^2 in {t_data:.1f} s")
@@ -268,18 +281,21 @@ def main(argv=None):
     torch.cuda.synchronize()
     t_train = time.time() - t0
     del xs, ts
-    res = {"train": {"phantoms": args.train, "noise": args.noise, "target_iters": args.target_iters, "epochs": args.epochs, "batch": args.batch, "lr": args.lr,
+    res = {"train": {"phantoms": args.train, "noise": args.noise, "target_iters": args.target_iters,
+                     "angles": args.angles, "mix_angles": args.mix_angles, "epochs": args.epochs, "batch": args.batch,
+                     "lr": args.lr,
                      "loss_per_epoch": hist, "data_s": t_data, "train_s": t_train,
                      "steps": args.epochs * (args.train // args.batch)}}
     res["eval_dense"] = evaluate(net, prob, args.eval, seed=777777, budgets=budgets, max_iters=args.max_iters,
                                  abs_targets=abs_t)
     log(json.dumps(res["eval_dense"]))
-    sparse = Problem(args.sparse_size, args.sparse_angles, noise=args.noise)
-    net512 = UNet(args.sparse_size, 8, seed=0)
-    net512.load(net.params())
-    res["eval_sparse_view"] = evaluate(net512, sparse, args.eval, seed=888888, budgets=budgets,
-                                       max_iters=args.max_iters, abs_targets=abs_t)
-    log(json.dumps(res["eval_sparse_view"]))
+    if not args.skip_sparse:
+        sparse = Problem(args.sparse_size, args.sparse_angles, noise=args.noise)
+        net512 = UNet(args.sparse_size, 8, seed=0)
+        net512.load(net.params())
+        res["eval_sparse_view"] = evaluate(net512, sparse, args.eval, seed=888888, budgets=budgets,
+                                           max_iters=args.max_iters, abs_targets=abs_t)
+        log(json.dumps(res["eval_sparse_view"]))
     if args.out:
         with open(args.out, "w") as f:
             json.dump(res, f, indent=1)
