@@ -75,22 +75,29 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
         if constexpr (UNIT) {
             float q = fmaf(xc, g.x, fmaf(-yc0, g.y, zoff));
             const float dq = -ystep * g.y;
+            // INRANGE: the address comes straight from the bits of the rounded
+            // sum r = q + 1.5*2^23 (bits(r) = bits(1.5*2^23) + s0), that constant
+            // folded into the row base: one wide multiply-add per gather pair
+            const uintptr_t rowb = reinterpret_cast<uintptr_t>(row) - (uintptr_t)kMagicBits * 4u;
 #pragma unroll
             for (int m = 0; m < PIX; ++m) {
                 if (m) q += dq;
-                int s0;
-                const float e = ceil_magic(q, s0) - q;
-                const float w0 = __saturatef(fmaf(-fabsf(e - fact), g.w, g.z));
-                const float w1 = __saturatef(fmaf(-e, g.w, le.y));
-                float v0, v1;
+                float v0, v1, e;
                 if constexpr (INRANGE) {
-                    const float *p = row + s0;
+                    const float r = __fadd_ru(q, kMagic);
+                    e = __fsub_rn(r, kMagic) - q;
+                    const float *p = reinterpret_cast<const float *>(
+                        rowb + (uintptr_t)(unsigned)__float_as_int(r) * 4u);
                     v0 = __ldg(p);
                     v1 = __ldg(p + 1);
                 } else {
+                    int s0;
+                    e = ceil_magic(q, s0) - q;
                     v0 = ((unsigned)s0 < uD) ? __ldg(row + s0) : 0.0f;
                     v1 = ((unsigned)(s0 + 1) < uD) ? __ldg(row + s0 + 1) : 0.0f;
                 }
+                const float w0 = __saturatef(fmaf(-fabsf(e - fact), g.w, g.z));
+                const float w1 = __saturatef(fmaf(-e, g.w, le.y));
                 if constexpr (SCALED) acc[m] = fmaf(w1, v1, fmaf(w0, v0, acc[m]));
                 else acc[m] = fmaf(le.x, fmaf(w1, v1, w0 * v0), acc[m]);
             }

@@ -281,51 +281,77 @@ __global__ void __launch_bounds__(256) row_scale_kernel(ProbGeom P, const float 
     sino_s[i] = sino[i] * row_scale(P.geom, k);
 }
 
+// Pixels per thread of the standalone backprojector (rows 8 apart: a block
+// covers 32 columns x 8*PIX rows), and the resident blocks per SM each variant
+// is compiled for.  8 pixels halve the per-angle overhead (dense data: 4.80 ms
+// against 5.02 at N = 2048, 2048 angles); 4 give twice the blocks, which the
+// few-angle (sparse-view) calls need.
+template <int PIX>
+struct BpShape {
+    static constexpr int kMinBlocks = PIX == 8 ? 5 : 6;
+};
+constexpr int kBpManyAngles = 256;     // angle count from which the 8-pixel variant runs
+
 // sino_s: the fast-path rows (scaled when SCALED, else sino itself); sino:
 // the unscaled rows read by the near-axis angles.
-template <bool UNIT, bool INRANGE, bool SCALED>
-__global__ void __launch_bounds__(256, 6) bp_tile_kernel(ProbGeom P, AngleLists L, const float *__restrict__ sino_s,
-                                                      const float *__restrict__ sino, float *__restrict__ out) {
+template <int kBpPix, bool UNIT, bool INRANGE, bool SCALED>
+__global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_tile_kernel(ProbGeom P, AngleLists L,
+                                                                   const float *__restrict__ sino_s,
+                                                                   const float *__restrict__ sino,
+                                                                   float *__restrict__ out) {
     __shared__ BpStage st;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int col = blockIdx.x * 32 + lane;
-    const int row0 = blockIdx.y * 32 + warp;
+    const int row0 = blockIdx.y * (8 * kBpPix) + warp;
     const float xc = (float)(col - P.half) + 0.5f;
     const float yc0 = (float)(row0 - P.half) + 0.5f;
-    float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f}, comp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    float sum[kBpPix], comp[kBpPix];
+#pragma unroll
+    for (int m = 0; m < kBpPix; ++m) sum[m] = comp[m] = 0.0f;
     for (int kc = 0; kc < P.a; kc += kBpChunk) {
         __syncthreads();
         bp_stage(P, kc, st);
         __syncthreads();
-        float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        bp_chunk<4, UNIT, INRANGE, SCALED>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
+        float part[kBpPix];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], part[m]);
+        for (int m = 0; m < kBpPix; ++m) part[m] = 0.0f;
+        bp_chunk<kBpPix, UNIT, INRANGE, SCALED>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
+#pragma unroll
+        for (int m = 0; m < kBpPix; ++m) comp_add(sum[m], comp[m], part[m]);
     }
-    float ex[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    bp_exact_angles<4>(P, L.exact, __ldg(L.counts + 2), 0, 1, sino, row0, 8, col, ex);
+    float ex[kBpPix];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < kBpPix; ++m) ex[m] = 0.0f;
+    bp_exact_angles<kBpPix>(P, L.exact, __ldg(L.counts + 2), 0, 1, sino, row0, 8, col, ex);
+#pragma unroll
+    for (int m = 0; m < kBpPix; ++m) {
         const int row = row0 + 8 * m;
         if (row < P.N && col < P.N) out[(size_t)row * P.N + col] = (sum[m] + comp[m]) + ex[m];
     }
 }
 
+template <int PIX>
+static void launch_bp_pix(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
+                          float *scaled) {
+    dim3 grid((P.N + 31) / 32, (P.N + 8 * PIX - 1) / (8 * PIX));
+    if (scaled) {
+        if (bp_windows_in_range(P)) bp_tile_kernel<PIX, true, true, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+        else if (P.deltarho == 1.0f)
+            bp_tile_kernel<PIX, true, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+        else bp_tile_kernel<PIX, false, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+    } else {
+        if (bp_windows_in_range(P)) bp_tile_kernel<PIX, true, true, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
+        else if (P.deltarho == 1.0f)
+            bp_tile_kernel<PIX, true, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
+        else bp_tile_kernel<PIX, false, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
+    }
+}
+
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
                       float *scaled) {
-    dim3 grid((P.N + 31) / 32, (P.N + 31) / 32);
-    if (scaled) {
-        row_scale_kernel<<<dim3((P.D + 255) / 256, P.a), 256, 0, stream>>>(P, sino, scaled);
-        if (bp_windows_in_range(P)) bp_tile_kernel<true, true, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
-        else if (P.deltarho == 1.0f)
-            bp_tile_kernel<true, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
-        else bp_tile_kernel<false, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
-    } else {
-        if (bp_windows_in_range(P)) bp_tile_kernel<true, true, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
-        else if (P.deltarho == 1.0f)
-            bp_tile_kernel<true, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
-        else bp_tile_kernel<false, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
-    }
+    if (scaled) row_scale_kernel<<<dim3((P.D + 255) / 256, P.a), 256, 0, stream>>>(P, sino, scaled);
+    if (P.a >= kBpManyAngles) launch_bp_pix<8>(P, L, sino, img, stream, scaled);
+    else launch_bp_pix<4>(P, L, sino, img, stream, scaled);
     return cudaGetLastError();
 }
 
