@@ -244,6 +244,7 @@ def run_gpu(args, rank, world):
     import torch
 
     from synkrotomo_gb300 import runtime as rt
+    from synkrotomo_gb300 import shard
 
     dev = torch.device("cuda", torch.cuda.current_device())
     g, img, sino = workload(seed=rank)
@@ -286,9 +287,7 @@ def run_gpu(args, rank, world):
     bp_ms = [b.elapsed_time(c) for _, b, c in ev]
     step_ms = sum(fp_ms) / len(fp_ms) + sum(bp_ms) / len(bp_ms)
     if world > 1:
-        t = torch.tensor([step_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+        step_ms = shard.max_over_ranks(step_ms)
         torch.distributed.barrier()
 
     # end to end through the public API, pinned host buffers

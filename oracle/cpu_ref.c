@@ -251,6 +251,9 @@ int cpuref_sirt(const float *angles, int a, float rhozero, float deltarho, const
     const int size = (int)sqrtf((float)n);      /* 16 */
     const int halfsize = size / 2;              /* 17 */
     const int numrhos = (int)(p / a);           /* 18 */
+    /* SIRT.fut:38-39 adds a (2*halfsize)^2-pixel backprojection to the n-pixel
+     * image: the shapes agree only for an even square side. */
+    if (size < 2 || (size & 1) || (int64_t)size * size != n) return 2;
     line_t *steep = malloc(sizeof(line_t) * (a + 1)), *flat = malloc(sizeof(line_t) * (a + 1));
     int *angle_index = malloc(sizeof(int) * (a + 1));
     unsigned char *ff = malloc(a + 1);
@@ -303,6 +306,7 @@ int cpuref_sirt3d(const float *angles, int a, const float *rhos, int r, const fl
     const float rhozero = rhos[0];
     const float deltarho = r > 1 ? rhos[1] - rhozero : 1.0f;
     const int64_t n = (int64_t)size * size;
+    if (size < 2 || (size & 1)) return 2;
     float *zero = calloc((size_t)n, sizeof(float));
     if (!zero) return 1;
     for (int i = 0; i < nslices; i++) {

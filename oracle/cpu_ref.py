@@ -78,13 +78,19 @@ def backprojection(angles, rhozero, deltarho, size, projections):
     return out
 
 
+def _check_sirt(rc, n):
+    if rc == 2:
+        raise ValueError(f"SIRT needs an even square image side (got {n} pixels)")
+    if rc:
+        raise MemoryError("cpu_ref: allocation failed")
+
+
 def sirt(angles, rhozero, deltarho, image, projections, iterations):
     angles, image, projections = _f32(angles), _f32(image), _f32(projections)
     out = np.empty(image.size, np.float32)
     rc = lib().cpuref_sirt(_p(angles), angles.size, float(rhozero), float(deltarho), _p(image), image.size,
                            _p(projections), projections.size, int(iterations), _p(out))
-    if rc:
-        raise MemoryError("cpu_ref: allocation failed")
+    _check_sirt(rc, image.size)
     return out
 
 
@@ -94,8 +100,7 @@ def sirt3d(angles, rhos, projections, iterations, size, nslices=None):
     out = np.empty(ns * int(size) * int(size), np.float32)
     rc = lib().cpuref_sirt3d(_p(angles), angles.size, _p(rhos), rhos.size, _p(projections), int(iterations),
                              int(size), ns, _p(out))
-    if rc:
-        raise MemoryError("cpu_ref: allocation failed")
+    _check_sirt(rc, int(size) ** 2)
     return out
 
 

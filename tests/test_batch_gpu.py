@@ -106,3 +106,31 @@ def test_sirt_plan_graph_replay(gpu):
             assert torch.equal(o, d.out)
         for p in probs:
             assert int(p.done[0].item()) == 25
+
+
+def test_sharded_drivers_single_rank_gpu(gpu):
+    """Without a process group the multi-rank drivers run the whole job on this
+    GPU: SIRT3D through the sharded driver equals SIRT3D bit for bit, and a
+    cost-split batch equals one batched launch."""
+    from synkrotomo_gb300 import shard
+    size, a, its = 32, 24, 12
+    g, b = _make(size, a, seed=7, nslices=size)
+    rhos = (np.float32(g.rhozero) + np.float32(g.deltarho) * np.arange(g.numrhos, dtype=np.float32))
+    ang_d, rhos_d, b_d = _dev(g.angles), _dev(rhos.astype(np.float32)), _dev(b)
+    ref = rt.sirt3d(ang_d, rhos_d, b_d, its, size)
+    vol = shard.sirt3d_sharded(ang_d, rhos_d, b_d, its, size)
+    assert torch.equal(vol, ref)
+
+    specs = [(64, 60, 15), (32, 30, 9), (48, 40, 11)]
+    made = [_make(s, n, seed=20 + i) for i, (s, n, _) in enumerate(specs)]
+    costs = [shard.problem_cost(n, g.numrhos, s, 1, it) for (s, n, it), (g, _) in zip(specs, made)]
+
+    def solve(idx):
+        probs = [rt.Problem(_dev(made[i][0].angles), made[i][0].rhozero, made[i][0].deltarho, made[i][0].numrhos,
+                            specs[i][0], _dev(made[i][1]), specs[i][2]) for i in idx]
+        return [p.out for p in rt.sirt_batch(probs)]
+
+    res = shard.batch_sharded(costs, solve)
+    ref = solve(list(range(len(specs))))
+    for x, y in zip(res, ref):
+        assert torch.equal(x, y)

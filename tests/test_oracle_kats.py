@@ -130,3 +130,18 @@ def test_sirt3d_oracles_agree():
     x32 = cpu_ref.sirt3d(g.angles, rhos, proj, 5, size)
     assert x64.shape == (size ** 3,)
     assert rel_l2(x32, x64) < 1e-5
+
+
+def test_cpu_sirt_rejects_odd_sides():
+    """SIRT.fut:38-39 adds a (2*halfsize)^2 backprojection to the n-pixel image,
+    so only even square sides are valid; the C restatement refuses the rest
+    (the product's C-ABI answers SYNK_EINVAL for them)."""
+    g = phantom.geometry(9, 6)
+    sino = np.zeros(6 * g.numrhos, np.float32)
+    with pytest.raises(ValueError):
+        cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(81, np.float32), sino, 2)
+    with pytest.raises(ValueError):
+        cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(80, np.float32), sino, 2)
+    rhos = np.float32(g.rhozero) + np.arange(g.numrhos, dtype=np.float32)
+    with pytest.raises(ValueError):
+        cpu_ref.sirt3d(g.angles, rhos, np.zeros(9 * sino.size, np.float32), 2, 9)
