@@ -202,20 +202,20 @@ int forward(synk_context *ctx, float *out, const float *angles, int64_t a, float
     cudaStream_t st = ctx->stream;
     Scratch sc(st);
     AngleGeom *geom;
-    float *xpad, *xTpad;
-    const size_t npad = (size_t)size * (size + 2);
-    SYNK_CUDA(sc.reserve(Scratch::round(sizeof(AngleGeom) * (size_t)a) + 2 * Scratch::round(sizeof(float) * npad) +
+    float2 *xpair, *xTpair;
+    const size_t npair = (size_t)size * (size + 2);
+    SYNK_CUDA(sc.reserve(Scratch::round(sizeof(AngleGeom) * (size_t)a) + 2 * Scratch::round(sizeof(float2) * npair) +
                          lists_bytes(a)),
               "cudaMallocAsync(scratch)");
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
-    SYNK_CUDA(sc.get(&xpad, (size_t)size * (size + 2)), "cudaMallocAsync(padded image)");
-    SYNK_CUDA(sc.get(&xTpad, (size_t)size * (size + 2)), "cudaMallocAsync(padded transposed image)");
+    SYNK_CUDA(sc.get(&xpair, npair), "cudaMallocAsync(pair image)");
+    SYNK_CUDA(sc.get(&xTpair, npair), "cudaMallocAsync(transposed pair image)");
     SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size, geom);
     AngleLists L;
     SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
-    SYNK_CUDA(launch_pad(image, xpad, xTpad, (int)size, 1, st), "pad kernel");
-    SYNK_CUDA(launch_fp(P, L, xpad, xTpad, out, st), "forward projection kernel");
+    SYNK_CUDA(launch_pair(image, xpair, xTpair, (int)size, st), "pair kernel");
+    SYNK_CUDA(launch_fp(P, L, xpair, xTpair, out, st), "forward projection kernel");
     return SYNK_OK;
 }
 

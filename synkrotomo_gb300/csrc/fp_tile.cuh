@@ -94,10 +94,67 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
     return k >= 0 ? (sum + comp) * g.lbase : 0.0f;
 }
 
+// fp_lane_ray on a pair image: pair[j*(N+2) + i] = (pad(j, i), pad(j, i+1) -
+// pad(j, i)) for i in [0, N+1], where pad(j, i) = pixel (j, i-1) and 0 outside
+// [1, N]; entry N+1 of every row is (0, 0).  One 8-byte gather per row serves
+// both pixels of the row segment (v0 + t*(v1 - v0) is one FMA on the entry).
+// Its index comes from the bits of r = u + kMagic rounded down,
+// c + 1 = bits(r) - (kMagicBits - 1), clamped as unsigned to N+1: a segment
+// left of column -1 wraps to a huge value and one right of N-1 exceeds N, and
+// both read the zero entry.  The loads are unconditional, so the rows of one
+// unrolled step issue their gathers back to back.
+__device__ __forceinline__ float fp_lane_ray_pair(const ProbGeom &P, int k, int r, const float2 *__restrict__ pair,
+                                                  int jb, int je) {
+    const AngleGeom g = load_geom(P.geom, k >= 0 ? k : 0);
+    const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));    // forwardprojection.fut:28
+    const float intercept = __fdiv_rn(rho, g.cost);                               // forwardprojection.fut:29
+    const float u0 = ray_u0(P, g, intercept);
+    int j0 = 0, j1 = 0;
+    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, u0, j0, j1);
+    j0 = max(j0, jb);
+    j1 = min(j1, je);
+    if (j1 <= j0) { j0 = je; j1 = je; }
+    const int J0 = __reduce_min_sync(0xffffffffu, j0);
+    const int J1 = __reduce_max_sync(0xffffffffu, j1);
+    const float slope = g.slope, ainv = g.ainv;
+    const uintptr_t rowbytes = (uintptr_t)(P.N + 2) * 8u;
+    const unsigned zix = (unsigned)P.N + 1u;                   // the zero entry of a row
+    const unsigned okbase = (unsigned)kMagicBits - 1u;         // bits(r) - okbase = c + 1
+    const uintptr_t base = reinterpret_cast<uintptr_t>(pair);
+    const float u1 = u0 + slope, u2 = u0 + 2.0f * slope, u3 = u0 + 3.0f * slope;
+    float sum = 0.0f, comp = 0.0f;
+    auto row = [&](float u, uintptr_t rowb, float &part) {
+        const float rr = __fadd_rd(u, kMagic);
+        const float fl = __fsub_rn(rr, kMagic);
+        const float t = right_share(u, fl, ainv);
+        const unsigned ix = min((unsigned)__float_as_int(rr) - okbase, zix);
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(rowb + (uintptr_t)ix * 8u));
+        part += fmaf(t, v.y, v.x);
+    };
+    for (int j = J0; j < J1;) {
+        const int jend = min(j + 32, J1);
+        float part = 0.0f;
+        float jf = (float)j;
+        uintptr_t rowb = base + (uintptr_t)j * rowbytes;
+        for (; j + 3 < jend; j += 4, jf += 4.0f, rowb += 4 * rowbytes) {
+            row(fmaf(jf, slope, u0), rowb, part);
+            row(fmaf(jf, slope, u1), rowb + rowbytes, part);
+            row(fmaf(jf, slope, u2), rowb + 2 * rowbytes, part);
+            row(fmaf(jf, slope, u3), rowb + 3 * rowbytes, part);
+        }
+        for (; j < jend; ++j, jf += 1.0f, rowb += rowbytes) row(fmaf(jf, slope, u0), rowb, part);
+        comp_add(sum, comp, part);
+    }
+    return k >= 0 ? (sum + comp) * g.lbase : 0.0f;
+}
+
 // Ray of a near-axis angle k, the reference's own expressions
 // (forwardprojection.fut:31-56), computed by the 32 lanes of a warp over the
 // frame rows [jb, je): lane l takes rows jb+l, jb+l+32, ...; the lane sums are
 // combined in a fixed order.  Returns the sum in every lane.
+// ESTEP 1: plain padded images (row stride N+2); ESTEP 2: pair images read
+// through their first halves (row stride 2*(N+2) floats).
+template <int ESTEP = 1>
 __device__ __forceinline__ float fp_exact_ray_warp(const ProbGeom &P, int k, int r, const float *__restrict__ xpad,
                                                    const float *__restrict__ xTpad, int jb = 0, int je = 1 << 30) {
     const int lane = threadIdx.x & 31;
@@ -105,11 +162,12 @@ __device__ __forceinline__ float fp_exact_ray_warp(const ProbGeom &P, int k, int
     const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));
     if (fabsf(rho) > 0.75f * (float)P.N + 2.0f) return 0.0f;
     const float intercept = __fdiv_rn(rho, g.cost);
-    const float *img = (g.flat ? xTpad : xpad) + 1;
+    const float *img = (g.flat ? xTpad : xpad) + ESTEP;
+    const int stride = ESTEP == 1 ? P.N + 2 : 2 * (P.N + 2);
     float acc = 0.0f;
     const int iend = min(P.half, -P.half + je);
     for (int i = -P.half + jb + lane; i < iend; i += 32)
-        acc = __fadd_rn(acc, fp_row_exact<false>(img, P.N + 2, P.half, g.slope, intercept, g.lbase, i));
+        acc = __fadd_rn(acc, fp_row_exact<false, ESTEP>(img, stride, P.half, g.slope, intercept, g.lbase, i));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
     return acc;
@@ -117,6 +175,7 @@ __device__ __forceinline__ float fp_exact_ray_warp(const ProbGeom &P, int k, int
 
 cudaError_t launch_angle_lists(const ProbGeom &P, int *order, int *exact, int *counts, cudaStream_t stream);
 cudaError_t launch_pad(const float *x, float *xpad, float *xTpad, int N, int nslices, cudaStream_t stream);
+cudaError_t launch_pair(const float *x, float2 *xpair, float2 *xTpair, int N, cudaStream_t stream);
 cudaError_t launch_unpad(const float *xpad, float *x, int N, int nslices, cudaStream_t stream);
 
 }  // namespace synk

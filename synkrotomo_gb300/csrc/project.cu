@@ -170,6 +170,48 @@ cudaError_t launch_pad(const float *x, float *xpad, float *xTpad, int N, int nsl
     return cudaGetLastError();
 }
 
+// Pair images of the forward projector: xpair[r][i] = (p(r, i), p(r, i+1) - p(r, i))
+// and xTpair[c][i] = (q(c, i), q(c, i+1) - q(c, i)) for i in [0, N+1] (row stride
+// N+2; entry N+1 is (0, 0)), where p(r, i) = x[r][i-1] and q(c, i) = x[i-1][c]
+// for i in [1, N], 0 otherwise: a row segment over pixels c, c+1 with share t
+// of c+1 adds first + t * second of entry c+1 (the difference rounds once, here).
+// Block (32, 8) covers i in [bx, bx+32) and rows r (columns c) in [by, by+32).
+// xpair reads its two values straight from x (coalesced along i); xTpair goes
+// through a tile of x rows bx-1 .. bx+31 so that its writes are coalesced too.
+__global__ void pair_kernel(const float *__restrict__ x, float2 *__restrict__ xpair, float2 *__restrict__ xTpair,
+                            int N) {
+    __shared__ float tile[33][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32, tx = threadIdx.x;
+    const int i = bx + tx;
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int r = by + y;
+        if (r < N && i <= N + 1) {
+            const float *xr = x + (size_t)r * N;
+            const float a = (i >= 1 && i <= N) ? xr[i - 1] : 0.0f;
+            const float b = (i < N) ? xr[i] : 0.0f;
+            xpair[(size_t)r * (N + 2) + i] = make_float2(a, __fsub_rn(b, a));
+        }
+    }
+    for (int y = threadIdx.y; y < 33; y += 8) {
+        const int row = bx - 1 + y, c = by + tx;
+        tile[y][tx] = (row >= 0 && row < N && c < N) ? x[(size_t)row * N + c] : 0.0f;
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int c = by + y;
+        if (c < N && i <= N + 1) {
+            const float a = tile[tx][y];
+            xTpair[(size_t)c * (N + 2) + i] = make_float2(a, __fsub_rn(tile[tx + 1][y], a));
+        }
+    }
+}
+
+cudaError_t launch_pair(const float *x, float2 *xpair, float2 *xTpair, int N, cudaStream_t stream) {
+    dim3 grid((N + 2 + 31) / 32, (N + 31) / 32);
+    pair_kernel<<<grid, dim3(32, 8), 0, stream>>>(x, xpair, xTpair, N);
+    return cudaGetLastError();
+}
+
 __global__ void unpad_kernel(const float *__restrict__ xpad, float *__restrict__ x, int N) {
     const size_t z = blockIdx.z;
     const int r = blockIdx.y;
@@ -189,8 +231,8 @@ cudaError_t launch_unpad(const float *xpad, float *x, int N, int nslices, cudaSt
 // angles (sparse-view data) the rays are split over rows so that enough warps
 // are in flight; the S partial sums of a ray are added in a fixed order.
 template <int S>
-__global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
-                                                      const float *__restrict__ xTpad, float *__restrict__ sino) {
+__global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, const float2 *__restrict__ xpair,
+                                                      const float2 *__restrict__ xTpair, float *__restrict__ sino) {
     __shared__ float red[8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int grp = blockIdx.y;
@@ -201,7 +243,7 @@ __global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, 
     const int rr = r < P.D ? r : P.D - 1;          // keep every warp for the block reduction
     const int k = __ldg(L.order + grp * 32 + lane);
     const int jb = part * P.N / S, je = (part + 1) * P.N / S;
-    float v = fp_lane_ray(P, r < P.D ? k : -1, rr, grp < nsteep ? xpad : xTpad, jb, je);
+    float v = fp_lane_ray_pair(P, r < P.D ? k : -1, rr, grp < nsteep ? xpair : xTpair, jb, je);
     if (S > 1) {
         red[warp][lane] = v;
         __syncthreads();
@@ -213,8 +255,10 @@ __global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, 
 
 // near-axis rays: a warp per (ray, row part), 8/S rays per block
 template <int S>
-__global__ void __launch_bounds__(256) fp_exact_kernel(ProbGeom P, AngleLists L, const float *__restrict__ xpad,
-                                                       const float *__restrict__ xTpad, float *__restrict__ sino) {
+__global__ void __launch_bounds__(256) fp_exact_kernel(ProbGeom P, AngleLists L, const float2 *__restrict__ xpair,
+                                                       const float2 *__restrict__ xTpair, float *__restrict__ sino) {
+    const float *xpad = reinterpret_cast<const float *>(xpair);
+    const float *xTpad = reinterpret_cast<const float *>(xTpair);
     __shared__ float red[8];
     const int nexact = __ldg(L.counts + 2);
     const int warp = threadIdx.x >> 5, part = warp % S;
@@ -222,7 +266,7 @@ __global__ void __launch_bounds__(256) fp_exact_kernel(ProbGeom P, AngleLists L,
     const int jb = part * P.N / S, je = (part + 1) * P.N / S;
     for (int e = blockIdx.y; e < nexact; e += gridDim.y) {      // block-uniform
         const int k = __ldg(L.exact + e);
-        float v = r < P.D ? fp_exact_ray_warp(P, k, r, xpad, xTpad, jb, je) : 0.0f;
+        float v = r < P.D ? fp_exact_ray_warp<2>(P, k, r, xpad, xTpad, jb, je) : 0.0f;
         if (S > 1) {
             __syncthreads();
             if ((threadIdx.x & 31) == 0) red[warp] = v;
@@ -243,17 +287,17 @@ static int fp_row_split(long long warps) {
     return S;
 }
 
-cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad, const float *xTpad, float *sino,
+cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float2 *xpair, const float2 *xTpair, float *sino,
                       cudaStream_t stream) {
     // groups of 32 angles: at most ceil(a/32) + 2 (the steep/flat split adds one partial group each)
     const int gmax = (P.a + 31) / 32 + 2;
     const int S = fp_row_split((long long)((P.a + 31) / 32) * P.D);
     const dim3 grid((P.D + 8 / S - 1) / (8 / S), gmax);
     switch (S) {
-        case 1: fp_lane_kernel<1><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
-        case 2: fp_lane_kernel<2><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
-        case 4: fp_lane_kernel<4><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
-        default: fp_lane_kernel<8><<<grid, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        case 1: fp_lane_kernel<1><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        case 2: fp_lane_kernel<2><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        case 4: fp_lane_kernel<4><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        default: fp_lane_kernel<8><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -261,10 +305,10 @@ cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad,
     const int SE = fp_row_split((long long)P.D * 2);
     const dim3 ge((P.D + 8 / SE - 1) / (8 / SE), 8);
     switch (SE) {
-        case 1: fp_exact_kernel<1><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
-        case 2: fp_exact_kernel<2><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
-        case 4: fp_exact_kernel<4><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
-        default: fp_exact_kernel<8><<<ge, 256, 0, stream>>>(P, L, xpad, xTpad, sino); break;
+        case 1: fp_exact_kernel<1><<<ge, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        case 2: fp_exact_kernel<2><<<ge, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        case 4: fp_exact_kernel<4><<<ge, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        default: fp_exact_kernel<8><<<ge, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
     }
     return cudaGetLastError();
 }

@@ -146,10 +146,11 @@ __device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int 
 // One frame row of the reference's own expressions (forwardprojection.fut:
 // 32-56), used for near-axis lines: every operation rounds exactly as the f32
 // reference.  Row i is centred (i in [-half, half)); img points at pixel (0, 0)
-// of the frame, rows `stride` floats apart.  When the segment stays in one
+// of the frame, rows `stride` floats apart, pixels ESTEP floats apart (2: the
+// first halves of a pair image).  When the segment stays in one
 // pixel the reference's two quotients are not used (lines 47, 54), so they are
 // only evaluated for two-pixel rows (xdiff can be 0 for an axis-parallel ray).
-template <bool ONES>
+template <bool ONES, int ESTEP = 1>
 __device__ __forceinline__ float fp_row_exact(const float *__restrict__ img, int stride, int half, float slope,
                                               float intercept, float lbase, int i) {
     const float xbot = __fadd_rn(__fmul_rn((float)i, slope), intercept);
@@ -171,9 +172,9 @@ __device__ __forceinline__ float fp_row_exact(const float *__restrict__ img, int
         if (botin) bot = lxbot;
         if (topin) top = lxtop;
     } else {
-        const float *row = img + (size_t)(i + half) * stride + half;
-        if (botin) bot = __fmul_rn(lxbot, __ldg(row + xpb));
-        if (topin) top = __fmul_rn(lxtop, __ldg(row + xpt));
+        const float *row = img + (size_t)(i + half) * stride + half * ESTEP;
+        if (botin) bot = __fmul_rn(lxbot, __ldg(row + xpb * ESTEP));
+        if (topin) top = __fmul_rn(lxtop, __ldg(row + xpt * ESTEP));
     }
     return __fadd_rn(bot, top);
 }
@@ -304,7 +305,7 @@ struct AngleLists;
 int device_sms();
 
 cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStream_t stream);
-cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float *xpad, const float *xTpad, float *sino,
+cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float2 *xpair, const float2 *xTpair, float *sino,
                       cudaStream_t stream);
 // scaled: scratch of a*D floats for the lbase-scaled rows (faster inner loop),
 // or null for the unscaled kernel (no scratch)
