@@ -656,7 +656,9 @@ def main():
                        "step": "forward projection + backprojection", "l2": "flushed (512 MB write) before every step",
                        "parallelism": f"replicas x{world}"},
             "fp_ms": res["fp_ms"], "bp_ms": res["bp_ms"],
-            "gpu_launches": 9 * args.steps,
+            # per step: setup (geometry_kernel when a > 1024, setup_kernel) + fp_lane_kernel + fp_exact_kernel
+            # (FP); setup + row_scale_kernel + bp_tile_kernel (BP)
+            "gpu_launches": (2 * (2 if N_ANGLES > 1024 else 1) + 4) * args.steps,
             "clocks": res["clocks"], "roofline": roofline}
     e = res["e2e"]
     if e is not None:

@@ -178,13 +178,19 @@ int pick_split(long long tasks, long long resident_warps, int max_split) {
 }
 
 // Angle lists of a geometry in scratch memory: order[a + 64], exact[a], counts[3].
-cudaError_t make_lists(Scratch &sc, const ProbGeom &P, AngleLists *L, cudaStream_t st) {
+// Geometry table and angle lists of P (P.geom must point at scratch of a
+// entries) in one setup launch; with x given, the same launch writes the pair
+// images of x for the forward projector.
+cudaError_t make_setup(Scratch &sc, const float *angles, const ProbGeom &P, AngleLists *L, cudaStream_t st,
+                       const float *x = nullptr, float2 *xpair = nullptr, float2 *xTpair = nullptr) {
     int *order, *exact, *counts;
     cudaError_t e;
     if ((e = sc.get(&order, (size_t)P.a + 64)) != cudaSuccess) return e;
     if ((e = sc.get(&exact, (size_t)P.a)) != cudaSuccess) return e;
     if ((e = sc.get(&counts, 4)) != cudaSuccess) return e;
-    if ((e = launch_angle_lists(P, order, exact, counts, st)) != cudaSuccess) return e;
+    if ((e = launch_setup(angles, P.a, const_cast<AngleGeom *>(P.geom), order, exact, counts, x, xpair, xTpair, P.N,
+                          st)) != cudaSuccess)
+        return e;
     L->order = order;
     L->exact = exact;
     L->counts = counts;
@@ -210,11 +216,9 @@ int forward(synk_context *ctx, float *out, const float *angles, int64_t a, float
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
     SYNK_CUDA(sc.get(&xpair, npair), "cudaMallocAsync(pair image)");
     SYNK_CUDA(sc.get(&xTpair, npair), "cudaMallocAsync(transposed pair image)");
-    SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size, geom);
     AngleLists L;
-    SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
-    SYNK_CUDA(launch_pair(image, xpair, xTpair, (int)size, st), "pair kernel");
+    SYNK_CUDA(make_setup(sc, angles, P, &L, st, image, xpair, xTpair), "setup kernel");
     SYNK_CUDA(launch_fp(P, L, xpair, xTpair, out, st), "forward projection kernel");
     return SYNK_OK;
 }
@@ -236,10 +240,9 @@ int backward(synk_context *ctx, float *out, const float *angles, int64_t a, floa
                          lists_bytes(a)),
               "cudaMallocAsync(scratch)");
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
-    SYNK_CUDA(launch_geometry(angles, (int)a, geom, st), "geometry kernel");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size_in, geom);
     AngleLists L;
-    SYNK_CUDA(make_lists(sc, P, &L, st), "angle lists");
+    SYNK_CUDA(make_setup(sc, angles, P, &L, st), "setup kernel");
     float *scaled;
     SYNK_CUDA(sc.get(&scaled, (size_t)p), "cudaMallocAsync(scaled rows)");
     SYNK_CUDA(launch_bp(P, L, projections, out, st, scaled), "backprojection kernel");
@@ -333,9 +336,8 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         SYNK_CUDA(cudaMemsetAsync(b2, 0, sizeof(double) * q.nslices, st), "memset");
         fill_i32_kernel<<<(unsigned)((q.nslices + 255) / 256), 256, 0, st>>>(stop_iter, q.nslices, INT_MAX);
         SYNK_CUDA(cudaGetLastError(), "fill kernel");
-        SYNK_CUDA(launch_geometry(q.angles, (int)q.a, geom, st), "geometry kernel");
         h.P = make_geom(q.a, q.rhozero, q.deltarho, q.numrhos, q.size, geom);
-        SYNK_CUDA(make_lists(sc, h.P, &h.L, st), "angle lists");
+        SYNK_CUDA(make_setup(sc, q.angles, h.P, &h.L, st), "setup kernel");
         SYNK_CUDA(launch_normalisers(h.P, R, C, st), "normaliser kernels");
         SYNK_CUDA(launch_pad(q.out, xpad, xTpad, q.size, q.nslices, st), "pad kernel");
         SYNK_CUDA(launch_sumsq(q.projections, pr, q.nslices, b2, st), "norm kernel");

@@ -175,7 +175,9 @@ __device__ __forceinline__ float fp_exact_ray_warp(const ProbGeom &P, int k, int
 
 cudaError_t launch_angle_lists(const ProbGeom &P, int *order, int *exact, int *counts, cudaStream_t stream);
 cudaError_t launch_pad(const float *x, float *xpad, float *xTpad, int N, int nslices, cudaStream_t stream);
-cudaError_t launch_pair(const float *x, float2 *xpair, float2 *xTpair, int N, cudaStream_t stream);
+// geometry table + angle lists (+ the pair images of x when x is not null) in one launch
+cudaError_t launch_setup(const float *angles, int a, AngleGeom *geom, int *order, int *exact, int *counts,
+                         const float *x, float2 *xpair, float2 *xTpair, int N, cudaStream_t stream);
 cudaError_t launch_unpad(const float *xpad, float *x, int N, int nslices, cudaStream_t stream);
 
 }  // namespace synk

@@ -1,12 +1,13 @@
 // Projector kernels of libsynk: per-angle geometry table, angle lists,
-// padded/transposed image copies, the forward projector
+// padded/transposed and pair image copies, the forward projector
 // (futhark/forwardprojection.fut:21-84), the backprojector
 // (futhark/backprojection.fut:19-93) and the SIRT normalisers
 // R = 1/(A*1), C = 1/(A^T*1) (futhark/SIRT.fut:22-25).
 //
+//   setup:    setup_kernel     geometry table + angle lists (+ pair images), one launch
 //   forward:  fp_lane_kernel   one warp = one detector x 32 angles of one class
 //             fp_exact_kernel  near-axis angles, the reference's expressions
-//   backward: bp_tile_kernel   one block = 32 x 32 pixels, 4 per thread, all angles
+//   backward: bp_tile_kernel   one block = 32 x 32 pixels, 4 or 8 per thread, all angles
 // See fp_tile.cuh and bp_tile.cuh for the per-ray and per-pixel arithmetic.
 #include <math.h>
 
@@ -32,10 +33,10 @@ int device_sms() {
 // and sin are evaluated in FP64 and rounded once, so they are the correctly
 // rounded float32 values that the reference's f32.cos / f32.sin return for
 // all practical inputs.
-__global__ void geometry_kernel(const float *__restrict__ angles, int a, AngleGeom *__restrict__ geom) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a) return;
-    const double th = (double)angles[k];
+// Geometry table entry of angle theta (every kernel that builds the table
+// uses this one function, so their tables are bit-identical).
+__device__ __forceinline__ AngleGeom angle_geometry(float theta) {
+    const double th = (double)theta;
     const float c = (float)cos(th);
     const float s = (float)sin(th);
     const bool flat = fabsf(s) >= fabsf(c);                       // sirtlib.fut:6-7
@@ -63,7 +64,13 @@ __global__ void geometry_kernel(const float *__restrict__ angles, int a, AngleGe
     // column receives it depends on how the reference's f32 expressions
     // round.  Those few angles run the reference's expressions verbatim.
     g.exact = asl < kExactSlope ? 1 : 0;
-    geom[k] = g;
+    return g;
+}
+
+__global__ void geometry_kernel(const float *__restrict__ angles, int a, AngleGeom *__restrict__ geom) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a) return;
+    geom[k] = angle_geometry(angles[k]);
 }
 
 cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStream_t stream) {
@@ -127,6 +134,145 @@ cudaError_t launch_angle_lists(const ProbGeom &P, int *order, int *exact, int *c
     return cudaGetLastError();
 }
 
+// Pair images of the forward projector: xpair[r][i] = (p(r, i), p(r, i+1) - p(r, i))
+// and xTpair[c][i] = (q(c, i), q(c, i+1) - q(c, i)) for i in [0, N+1] (row stride
+// N+2; entry N+1 is (0, 0)), where p(r, i) = x[r][i-1] and q(c, i) = x[i-1][c]
+// for i in [1, N], 0 otherwise: a row segment over pixels c, c+1 with share t
+// of c+1 adds first + t * second of entry c+1 (the difference rounds once, here).
+//
+// One launch for everything a projection needs before its main kernel.
+// Block 0 builds the geometry table (unless have_geom: the table is already
+// written) and the angle lists of angle_lists_kernel (same layout and order)
+// with warp ballots: pass 1 writes the table and counts the classes, pass 2
+// re-reads the class flags and writes every angle at its ordered position.  Blocks 1.. (when x is given) write the pair images,
+// one tile of 32 entries x 32 rows each, while block 0 works: xpair reads its
+// two values straight from x (coalesced along i), xTpair goes through a tile
+// of x rows bx-1 .. bx+31 so that its writes are coalesced too.
+__global__ void __launch_bounds__(1024) setup_kernel(const float *__restrict__ angles, int a,
+                                                     AngleGeom *__restrict__ geom, int *__restrict__ order,
+                                                     int *__restrict__ exact, int *__restrict__ counts,
+                                                     const float *__restrict__ x, float2 *__restrict__ xpair,
+                                                     float2 *__restrict__ xTpair, int N, bool have_geom) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (blockIdx.x == 0) {
+        __shared__ int tot[3];
+        __shared__ int woff[3][32];
+        __shared__ int ctot[3];
+        if (tid < 3) tot[tid] = 0;
+        __syncthreads();
+        for (int k0 = 0; k0 < a; k0 += 1024) {                  // pass 1
+            const int k = k0 + tid;
+            int cls = 3;
+            if (k < a) {
+                if (have_geom) {
+                    const int *gi = reinterpret_cast<const int *>(geom + k);
+                    cls = gi[11] ? 2 : gi[10];                    // exact, flat
+                } else {
+                    const AngleGeom g = angle_geometry(angles[k]);
+                    geom[k] = g;
+                    cls = g.exact ? 2 : g.flat;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const unsigned b = __ballot_sync(0xffffffffu, cls == c);
+                if (lane == 0 && b) atomicAdd(&tot[c], __popc(b));
+            }
+        }
+        __syncthreads();
+        const int gs = (tot[0] + 31) / 32, gf = (tot[1] + 31) / 32;
+        const unsigned below = (1u << lane) - 1u;
+        int base0 = 0, base1 = 0, base2 = 0;
+        for (int k0 = 0; k0 < a; k0 += 1024) {                  // pass 2
+            const int k = k0 + tid;
+            int cls = 3;
+            if (k < a) {
+                const int *gi = reinterpret_cast<const int *>(geom + k);
+                cls = gi[11] ? 2 : gi[10];                        // exact, flat
+            }
+            unsigned b[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) b[c] = __ballot_sync(0xffffffffu, cls == c);
+            if (lane == 0) {
+                woff[0][w] = __popc(b[0]);
+                woff[1][w] = __popc(b[1]);
+                woff[2][w] = __popc(b[2]);
+            }
+            __syncthreads();
+            if (w < 3) {                                          // exclusive scan of the 32 warp counts
+                const int v = woff[w][lane];
+                int incl = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                woff[w][lane] = incl - v;
+                if (lane == 31) ctot[w] = incl;
+            }
+            __syncthreads();
+            if (cls == 0) order[base0 + woff[0][w] + __popc(b[0] & below)] = k;
+            else if (cls == 1) order[gs * 32 + base1 + woff[1][w] + __popc(b[1] & below)] = k;
+            else if (cls == 2) exact[base2 + woff[2][w] + __popc(b[2] & below)] = k;
+            base0 += ctot[0];
+            base1 += ctot[1];
+            base2 += ctot[2];
+            __syncthreads();
+        }
+        if (tid < 32) {
+            if (tot[0] + tid < gs * 32) order[tot[0] + tid] = -1;
+            if (tot[1] + tid < gf * 32) order[gs * 32 + tot[1] + tid] = -1;
+        }
+        if (tid == 0) {
+            counts[0] = gs;
+            counts[1] = gf;
+            counts[2] = tot[2];
+        }
+        return;
+    }
+    // pair tiles: i in [bx, bx+32) of pair rows [by, by+32)
+    __shared__ float tile[33][33];
+    const int tiles_x = (N + 2 + 31) / 32;
+    const int t = blockIdx.x - 1;
+    const int bx = (t % tiles_x) * 32, by = (t / tiles_x) * 32;
+    const int i = bx + lane;
+    {
+        const int r = by + w;
+        if (r < N && i <= N + 1) {
+            const float *xr = x + (size_t)r * N;
+            const float va = (i >= 1 && i <= N) ? xr[i - 1] : 0.0f;
+            const float vb = (i < N) ? xr[i] : 0.0f;
+            xpair[(size_t)r * (N + 2) + i] = make_float2(va, __fsub_rn(vb, va));
+        }
+    }
+    for (int y = w; y < 33; y += 32) {
+        const int row = bx - 1 + y, c = by + lane;
+        tile[y][lane] = (row >= 0 && row < N && c < N) ? x[(size_t)row * N + c] : 0.0f;
+    }
+    __syncthreads();
+    const int c = by + w;
+    if (c < N && i <= N + 1) {
+        const float va = tile[lane][w];
+        xTpair[(size_t)c * (N + 2) + i] = make_float2(va, __fsub_rn(tile[lane + 1][w], va));
+    }
+}
+
+cudaError_t launch_setup(const float *angles, int a, AngleGeom *geom, int *order, int *exact, int *counts,
+                         const float *x, float2 *xpair, float2 *xTpair, int N, cudaStream_t stream) {
+    // Beyond one block's worth of angles the table's FP64 trigonometry is
+    // spread over the geometry kernel's blocks first, and block 0 only reads
+    // the class flags.
+    const bool have_geom = a > 1024;
+    if (have_geom) {
+        cudaError_t e = launch_geometry(angles, a, geom, stream);
+        if (e != cudaSuccess) return e;
+    }
+    const int tiles = x ? ((N + 2 + 31) / 32) * ((N + 31) / 32) : 0;
+    setup_kernel<<<1 + tiles, 1024, 0, stream>>>(angles, a, geom, order, exact, counts, x, xpair, xTpair, N,
+                                                 have_geom);
+    return cudaGetLastError();
+}
+
 // xpad[z][r][c+1] = x[z][r][c], xTpad[z][c][r+1] = x[z][r][c] (row stride N+2);
 // the blocks of the first and last tile column (row) also write the zero pad
 // columns 0 and N+1 of their rows of xpad (xTpad).
@@ -167,48 +313,6 @@ __global__ void pad_kernel(const float *__restrict__ x, float *__restrict__ xpad
 cudaError_t launch_pad(const float *x, float *xpad, float *xTpad, int N, int nslices, cudaStream_t stream) {
     dim3 grid((N + 31) / 32, (N + 31) / 32, nslices);
     pad_kernel<<<grid, dim3(32, 8), 0, stream>>>(x, xpad, xTpad, N);
-    return cudaGetLastError();
-}
-
-// Pair images of the forward projector: xpair[r][i] = (p(r, i), p(r, i+1) - p(r, i))
-// and xTpair[c][i] = (q(c, i), q(c, i+1) - q(c, i)) for i in [0, N+1] (row stride
-// N+2; entry N+1 is (0, 0)), where p(r, i) = x[r][i-1] and q(c, i) = x[i-1][c]
-// for i in [1, N], 0 otherwise: a row segment over pixels c, c+1 with share t
-// of c+1 adds first + t * second of entry c+1 (the difference rounds once, here).
-// Block (32, 8) covers i in [bx, bx+32) and rows r (columns c) in [by, by+32).
-// xpair reads its two values straight from x (coalesced along i); xTpair goes
-// through a tile of x rows bx-1 .. bx+31 so that its writes are coalesced too.
-__global__ void pair_kernel(const float *__restrict__ x, float2 *__restrict__ xpair, float2 *__restrict__ xTpair,
-                            int N) {
-    __shared__ float tile[33][33];
-    const int bx = blockIdx.x * 32, by = blockIdx.y * 32, tx = threadIdx.x;
-    const int i = bx + tx;
-    for (int y = threadIdx.y; y < 32; y += 8) {
-        const int r = by + y;
-        if (r < N && i <= N + 1) {
-            const float *xr = x + (size_t)r * N;
-            const float a = (i >= 1 && i <= N) ? xr[i - 1] : 0.0f;
-            const float b = (i < N) ? xr[i] : 0.0f;
-            xpair[(size_t)r * (N + 2) + i] = make_float2(a, __fsub_rn(b, a));
-        }
-    }
-    for (int y = threadIdx.y; y < 33; y += 8) {
-        const int row = bx - 1 + y, c = by + tx;
-        tile[y][tx] = (row >= 0 && row < N && c < N) ? x[(size_t)row * N + c] : 0.0f;
-    }
-    __syncthreads();
-    for (int y = threadIdx.y; y < 32; y += 8) {
-        const int c = by + y;
-        if (c < N && i <= N + 1) {
-            const float a = tile[tx][y];
-            xTpair[(size_t)c * (N + 2) + i] = make_float2(a, __fsub_rn(tile[tx + 1][y], a));
-        }
-    }
-}
-
-cudaError_t launch_pair(const float *x, float2 *xpair, float2 *xTpair, int N, cudaStream_t stream) {
-    dim3 grid((N + 2 + 31) / 32, (N + 31) / 32);
-    pair_kernel<<<grid, dim3(32, 8), 0, stream>>>(x, xpair, xTpair, N);
     return cudaGetLastError();
 }
 
@@ -253,13 +357,17 @@ __global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, 
     if (k >= 0 && r < P.D) sino[(size_t)k * P.D + r] = v;
 }
 
-// near-axis rays: a warp per (ray, row part), 8/S rays per block
+// Near-axis rays (the reference's own expressions, on the pair images' first
+// halves): a warp per (ray, row part), 8/S rays per block, kExactSlots angle
+// slots (at most four near-axis angles lie in [0, 2 pi); repeats loop).
+constexpr int kExactSlots = 4;
+
 template <int S>
 __global__ void __launch_bounds__(256) fp_exact_kernel(ProbGeom P, AngleLists L, const float2 *__restrict__ xpair,
                                                        const float2 *__restrict__ xTpair, float *__restrict__ sino) {
+    __shared__ float red[8];
     const float *xpad = reinterpret_cast<const float *>(xpair);
     const float *xTpad = reinterpret_cast<const float *>(xTpair);
-    __shared__ float red[8];
     const int nexact = __ldg(L.counts + 2);
     const int warp = threadIdx.x >> 5, part = warp % S;
     const int r = blockIdx.x * (8 / S) + warp / S;
@@ -301,9 +409,9 @@ cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float2 *xpai
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    // near-axis angles: at most 4 in [0, 2 pi); rays x 8 angle slots must fill the GPU
+    // near-axis angles: rays x angle slots must fill the GPU
     const int SE = fp_row_split((long long)P.D * 2);
-    const dim3 ge((P.D + 8 / SE - 1) / (8 / SE), 8);
+    const dim3 ge((P.D + 8 / SE - 1) / (8 / SE), kExactSlots);
     switch (SE) {
         case 1: fp_exact_kernel<1><<<ge, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
         case 2: fp_exact_kernel<2><<<ge, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;

@@ -125,3 +125,25 @@ def test_large_geometry_against_fp64_oracle_sample(gpu):
     ref64 = F.forwardprojection(angles, rhozero, 1.0, nr, img)
     assert rel_l2(out, ref32) < TOL
     assert rel_l2(out, ref64) < TOL
+
+
+def test_many_angles_and_repeated_axis_angles(gpu):
+    """2503 angles: three 1024-angle chunks of the setup kernel's lists, all four
+    axis directions of [0, 2 pi) plus three repeats (seven near-axis angles,
+    more than the near-axis kernel's angle slots), in an unsorted order."""
+    size = 64
+    base = np.linspace(0.0, 2 * math.pi, 2500, endpoint=False).astype(np.float32)
+    extra = np.array([0.0, np.float32(math.pi / 2), np.float32(math.pi)], np.float32)
+    ang = np.concatenate([base[::-1], extra, base[:0]]).astype(np.float32)
+    rng = np.random.default_rng(3)
+    ang = ang[rng.permutation(ang.size)].copy()
+    g = phantom.geometry(size, 1)
+    img = phantom.ellipse_phantom(size, seed=21)
+    out = rt.forwardprojection(_dev(ang), g.rhozero, 1.0, g.numrhos, _dev(img)).cpu().numpy()
+    ref32 = cpu_ref.forwardprojection(ang, g.rhozero, 1.0, g.numrhos, img)
+    assert rel_l2(out, ref32) < TOL
+    assert np.max(np.abs(out - ref32)) <= 1e-4 * max(1.0, float(np.max(np.abs(ref32))))
+    y = rng.random(ang.size * g.numrhos).astype(np.float32)
+    bt = rt.backprojection(_dev(ang), g.rhozero, 1.0, size, _dev(y)).cpu().numpy()
+    ref_bt = cpu_ref.backprojection(ang, g.rhozero, 1.0, size, y)
+    assert rel_l2(bt, ref_bt) < TOL
