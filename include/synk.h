@@ -116,7 +116,11 @@ typedef struct synk_sirt_options {
     /* Rows (FP) / angles (BP) split per work item: 0 = automatic. */
     int32_t fp_split;
     int32_t bp_split;
-    /* Blocks of the persistent launch: 0 = every block that fits on the GPU. */
+    /* Engine and grid: > 0 = the persistent kernel with that many blocks;
+     * 0 = automatic (one launch per phase and iteration when an iteration is
+     * small: at most 6e7 ray-row steps plus pixel-angle pairs, e.g. a few
+     * slices of N <= 256; otherwise the persistent kernel with every block
+     * that fits); -1 = one launch per phase and iteration. */
     int32_t grid_blocks;
 } synk_sirt_options;
 
@@ -163,7 +167,9 @@ int synk_sirt_batch(synk_context *ctx, int32_t nprob, const synk_sirt_problem *p
 /* A batched SIRT solve captured once in a CUDA graph (with its own scratch)
  * and replayed by synk_sirt_plan_launch on the context's stream.  The arrays
  * of `probs` are bound at creation: change their contents between launches,
- * not the pointers. */
+ * not the pointers.  grid_blocks 0 selects the persistent kernel here (a
+ * captured phase-split loop cannot end early); -1 captures one launch per
+ * phase and iteration. */
 typedef struct synk_sirt_plan synk_sirt_plan;
 int synk_sirt_plan_new(synk_context *ctx, synk_sirt_plan **out, int32_t nprob, const synk_sirt_problem *probs,
                        double tol, int32_t grid_blocks);

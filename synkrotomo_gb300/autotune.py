@@ -5,7 +5,8 @@ Tunables per problem:
                8/fp_split detectors (x 32 angles) per block item
   bp_split     1/2/4/8 warps share one pixel strip of the backward phase
                (angles split); tiles of 32 x 4*8/bp_split pixels
-  grid_blocks  blocks of the cooperative launch (all resident, or half)
+  grid_blocks  blocks of the cooperative launch (all resident, or half), or
+               -1: the phase-split engine (one launch per phase and iteration)
 Each candidate is timed on the problem itself (a few iterations, CUDA events);
 the winner is cached in a JSON file keyed by the size bucket
 (image side, angle count, detector count, slices rounded to powers of two), so
@@ -63,7 +64,7 @@ def save_cache(cache: dict, path: str | None = None) -> None:
 def candidates(size: int, n_angles: int, resident_blocks: int):
     fs = [s for s in SPLITS if s == 1 or size // s >= 16]
     bs = [s for s in SPLITS if s == 1 or n_angles // s >= 8]
-    grids = sorted({resident_blocks, max(1, resident_blocks // 2)})
+    grids = sorted({resident_blocks, max(1, resident_blocks // 2)}) + [-1]
     return [dict(fp_split=f, bp_split=b, grid_blocks=g) for f, b, g in itertools.product(fs, bs, grids)]
 
 

@@ -321,6 +321,39 @@ __global__ void __launch_bounds__(256, 3) sirt_persistent_kernel(SirtParams p) {
     }
 }
 
+// Phase-split engine: the same two phases as ordinary launches, one per phase
+// and iteration.  The kernel boundary replaces the grid barrier, which for
+// small iterations (a few slices of N <= 256) is cheaper than the persistent
+// kernel's two barriers per iteration; each kernel also gets its own register
+// allocation.  Items are assigned statically (item = block + i*grid).
+__global__ void __launch_bounds__(256, 5) sirt_fp_phase_kernel(SirtParams p, int it) {
+    __shared__ SirtShared sh;
+    fp_phase(p, it, nullptr, sh);
+}
+
+// Block 0 also applies the stopping rule of iteration it (the same decision
+// as the fused kernel: every block's bp_needed reads the same residuals) and
+// stores the number of slices still updating in *active.
+__global__ void __launch_bounds__(256, 4) sirt_bp_phase_kernel(SirtParams p, int it, int *active) {
+    __shared__ SirtShared sh;
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) sh.any = 0;
+        __syncthreads();
+        int cnt = 0;
+        for (int qi = 0; qi < p.nprob; ++qi) {
+            const SirtProblem &q = p.probs[qi];
+            for (int s = threadIdx.x; s < q.nslices; s += blockDim.x) {
+                if (bp_needed(p, q, s, it)) ++cnt;
+                else if (p.tol2 > 0.0 && it < q.iterations && stop_of(q, s) > it) q.stop_iter[s] = it;
+            }
+        }
+        if (cnt) atomicAdd(&sh.any, cnt);
+        __syncthreads();
+        if (threadIdx.x == 0) *active = sh.any;
+    }
+    bp_phase(p, it, nullptr, sh);
+}
+
 // Per-problem item counts and begin offsets (depend on the angle lists).
 __global__ void sirt_plan_kernel(SirtProblem *probs, int nprob, long long *totals) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -403,6 +436,27 @@ int sirt_persistent_grid(int *blocks_per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sirt_persistent_kernel, 256, 0);
     if (blocks_per_sm) *blocks_per_sm = bps;
     return sms * bps;
+}
+
+int sirt_phase_grids(int *fp_grid, int *bp_grid) {
+    int dev = 0, sms = 0, f = 0, b = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, sirt_fp_phase_kernel, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sirt_bp_phase_kernel, 256, 0);
+    *fp_grid = sms * f;
+    *bp_grid = sms * b;
+    return f > 0 && b > 0;
+}
+
+cudaError_t launch_sirt_fp_phase(const SirtParams &p, int it, int grid, cudaStream_t stream) {
+    sirt_fp_phase_kernel<<<grid, 256, 0, stream>>>(p, it);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sirt_bp_phase(const SirtParams &p, int it, int *active, int grid, cudaStream_t stream) {
+    sirt_bp_phase_kernel<<<grid, 256, 0, stream>>>(p, it, active);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sirt_persistent(const SirtParams &p, int grid, cudaStream_t stream) {

@@ -51,6 +51,10 @@ cudaError_t launch_sumsq(const float *b, size_t len, int nslices, double *out, c
 cudaError_t launch_sirt_plan(SirtProblem *probs, int nprob, long long *totals, cudaStream_t stream);
 int sirt_persistent_grid(int *blocks_per_sm);
 cudaError_t launch_sirt_persistent(const SirtParams &p, int grid, cudaStream_t stream);
+// phase-split engine: resident grids of the two phase kernels, and their launches
+int sirt_phase_grids(int *fp_grid, int *bp_grid);
+cudaError_t launch_sirt_fp_phase(const SirtParams &p, int it, int grid, cudaStream_t stream);
+cudaError_t launch_sirt_bp_phase(const SirtParams &p, int it, int *active, int grid, cudaStream_t stream);
 cudaError_t launch_sirt_finalize(SirtProblem *probs, int nprob, int max_slices, int record_final,
                                  cudaStream_t stream);
 

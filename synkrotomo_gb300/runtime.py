@@ -259,6 +259,14 @@ class Problem:
                                 self.done.data_ptr(), self.fp_split, self.bp_split)
 
 
+def resident_blocks() -> int:
+    """Blocks of the persistent SIRT kernel that fit on the device at once:
+    ``grid_blocks`` of that value forces the persistent engine with its full
+    grid, -1 the phase-split engine, 0 lets the library choose."""
+    context()
+    return int(_lib.load().synk_sirt_resident_blocks())
+
+
 def sirt_batch(problems: list, tol: float = 0.0, grid_blocks: int = 0) -> list:
     """Every problem's SIRT in one persistent launch (``synk_sirt_batch``);
     results land in each problem's ``out`` / ``residuals`` / ``done``."""

@@ -11,7 +11,7 @@ def test_candidates_respect_minimum_work():
     c = autotune.candidates(32, 16, 304)
     assert {x["fp_split"] for x in c} == {1, 2}          # 32 rows: at least 16 rows per part
     assert {x["bp_split"] for x in c} == {1, 2}          # 16 angles: at least 8 per part
-    assert {x["grid_blocks"] for x in c} == {152, 304}
+    assert {x["grid_blocks"] for x in c} == {152, 304, -1}   # -1: the phase-split engine
 
 
 def test_choose_measures_once_then_reads_the_cache(tmp_path):

@@ -113,3 +113,52 @@ def test_sirt3d_matches_reference_semantics(gpu):
     ref = cpu_ref.sirt3d(g.angles, rhos, proj, 8, size)
     assert x.shape == (size ** 3,)
     assert rel_l2(x, ref) < 1e-5
+
+
+def test_phase_split_engine_matches_persistent(gpu):
+    """grid_blocks=-1 runs one launch per phase and iteration.  The same items
+    compute the same values, so without a stopping rule the iterates are
+    bit-identical to the persistent kernel's; with one, every slice stops at
+    the same iteration (the loop then ends on the host's check of the active
+    count after iteration 16, 32, ...)."""
+    size, a, ns, its = 48, 40, 6, 45
+    g = phantom.geometry(size, a)
+    vol = phantom.ellipsoid_volume(size, ns, seed=3)
+    sinos = np.stack([cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, vol[i])
+                      for i in range(ns)])
+    ang, bd = _dev(g.angles), _dev(sinos.ravel())
+    full = rt.resident_blocks()
+    xp, rp, dp = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
+                                grid_blocks=full)
+    xs, rs, ds = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
+                                grid_blocks=-1)
+    assert torch.equal(xp, xs)
+    assert torch.equal(dp, ds)
+    np.testing.assert_allclose(rs.cpu().numpy(), rp.cpu().numpy(), rtol=1e-12)
+    ref = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), sinos[2], its)
+    assert rel_l2(xs.cpu().numpy().reshape(ns, -1)[2], ref) < 1e-5
+    # stopping rule: per-slice stops between iteration 8 and 30
+    hist = rp.cpu().numpy()
+    tol = float(np.median(hist[:, 20]))
+    xp2, _, dp2 = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, tol=tol,
+                                 grid_blocks=full)
+    xs2, _, ds2 = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, tol=tol,
+                                 grid_blocks=-1)
+    assert torch.equal(dp2, ds2)
+    assert torch.equal(xp2, xs2)
+    assert int(ds2.min()) < its and int(ds2.max()) > 16
+
+
+def test_phase_split_engine_uneven_batch(gpu):
+    specs = [(64, 60, 20), (32, 90, 35), (48, 17, 10)]
+    probs, refs = [], []
+    for i, (size, a, its) in enumerate(specs):
+        g, _, b = _problem(size, a, seed=30 + i)
+        probs.append(rt.Problem(_dev(g.angles), g.rhozero, g.deltarho, g.numrhos, size, _dev(b), its))
+        refs.append(cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), b, its))
+    rt.sirt_batch(probs, grid_blocks=-1)
+    for p, ref, spec in zip(probs, refs, specs):
+        assert rel_l2(p.out.cpu().numpy(), ref) < 1e-5, spec
+        assert int(p.done.item()) == spec[2]
+    with pytest.raises(ValueError):
+        rt.sirt_batch(probs, grid_blocks=-2)
