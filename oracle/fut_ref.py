@@ -231,6 +231,38 @@ def bp_matrix(angles, rhozero, deltarho, numrhos, size, count_oob=False):
     return (m, oob) if count_oob else m
 
 
+def backprojection_rows(angles, rhozero, deltarho, size, projections, rows):
+    """Rows ``rows`` of backprojection.fut:82-93 ``main`` ([len(rows), size]),
+    from the same per-pixel rule as ``bp_matrix`` without building the matrix:
+    for a steep line an image row is a frame row; a flat line works in the
+    transposed frame (lines 75-78), where the image row is a frame column."""
+    halfsize = int(size) // 2
+    rz = float(np.float32(rhozero))
+    dr = float(np.float32(deltarho))
+    rpp = rhos_per_pixel(deltarho)
+    proj = np.asarray(projections, dtype=np.float32).astype(np.float64)
+    a = np.asarray(angles).size
+    numrhos = proj.size // a
+    cost, sint, lbase, flat = preprocess(angles)
+    rows = np.asarray(rows, dtype=np.int64)
+    coords = np.arange(-halfsize, halfsize, dtype=np.float64)
+    fixed = rows.astype(np.float64)[:, None] - halfsize          # [R, 1]
+    out = np.zeros((rows.size, int(size)))
+    for k in range(cost.size):
+        if flat[k]:
+            xmin, ymin = np.broadcast_to(fixed, out.shape), np.broadcast_to(coords[None, :], out.shape)
+        else:
+            ymin, xmin = np.broadcast_to(fixed, out.shape), np.broadcast_to(coords[None, :], out.shape)
+        s = first_detector(cost[k], sint[k], xmin, ymin, rz, dr)
+        for i in range(rpp):
+            sprime = s + i
+            w = bp_weight(cost[k], sint[k], lbase[k], xmin, ymin, sprime, rz, dr)
+            det = sprime.astype(np.int64)
+            ok = (det >= 0) & (det < numrhos) & (w != 0.0)
+            out += np.where(ok, w * proj[k * numrhos + np.clip(det, 0, numrhos - 1)], 0.0)
+    return out
+
+
 def backprojection(angles, rhozero, deltarho, size, projections):
     """backprojection.fut:82-93 ``main``: image [size*size]."""
     projections = np.asarray(projections, dtype=np.float32)

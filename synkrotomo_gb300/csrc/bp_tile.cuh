@@ -73,7 +73,11 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
         const float2 le = st.le[i];
         const float *__restrict__ row = sino + (size_t)(kc + i) * D;
         if constexpr (UNIT) {
-            float q = fmaf(xc, g.x, fmaf(-yc0, g.y, zoff));
+            // q of pixel m from the angle's base value in one rounding
+            // (fma(m, dq, q0)), not by repeated additions: those drift by up
+            // to PIX-1 roundings of |q| ~ D/2, which near-axis-adjacent
+            // angles (trapezoid edges 1/b steep) turn into visible weight errors
+            const float q0 = fmaf(xc, g.x, fmaf(-yc0, g.y, zoff));
             const float dq = -ystep * g.y;
             // INRANGE: the address comes straight from the bits of the rounded
             // sum r = q + 1.5*2^23 (bits(r) = bits(1.5*2^23) + s0), that constant
@@ -81,7 +85,7 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
             const uintptr_t rowb = reinterpret_cast<uintptr_t>(row) - (uintptr_t)kMagicBits * 4u;
 #pragma unroll
             for (int m = 0; m < PIX; ++m) {
-                if (m) q += dq;
+                const float q = m ? fmaf((float)m, dq, q0) : q0;
                 float v0, v1, e;
                 if constexpr (INRANGE) {
                     const float r = __fadd_ru(q, kMagic);
@@ -102,10 +106,11 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
                 else acc[m] = fmaf(le.x, fmaf(w1, v1, w0 * v0), acc[m]);
             }
         } else {
-            float t = fmaf(-yc0, g.y, -P.rhozero);
+            const float t0 = fmaf(-yc0, g.y, -P.rhozero);
             const float tstep = -ystep * g.y;
 #pragma unroll
-            for (int m = 0; m < PIX; ++m, t += tstep) {
+            for (int m = 0; m < PIX; ++m) {
+                const float t = m ? fmaf((float)m, tstep, t0) : t0;
                 const float qc = fmaf(xc, g.x, t);             // rho_c - rhozero
                 int s0;
                 float s0f = ceil_magic((qc - fact) * P.inv_deltarho, s0);
@@ -131,11 +136,15 @@ __device__ __forceinline__ float row_scale(const AngleGeom *__restrict__ geom, i
 // True when every pixel's two candidate detectors of the UNIT path lie in
 // [0, D) (deltarho = 1 and a detector row covering the image's circumcircle,
 // as the reference's D >= ceil(N*sqrt(2)) with centred rhozero does).  The
-// tiles cover rows and columns [0, 32*ceil(N/32)), so the bound takes the
-// padded extent, and it keeps a margin for the float rounding of q.
-inline bool bp_windows_in_range(const ProbGeom &P) {
+// tiles cover columns [0, 32*ceil(N/32)) and rows [0, tile_rows*ceil(N/tile_rows))
+// (pixels past N are computed, not stored), so the bound takes the padded
+// extent, and it keeps a margin for the float rounding of q.  A launch whose
+// tile height divides tile_rows never reaches further.
+inline bool bp_windows_in_range(const ProbGeom &P, int tile_rows) {
     if (P.deltarho != 1.0f) return false;
-    const int ext = (P.N + 31) / 32 * 32;
+    const int ext_x = (P.N + 31) / 32 * 32;
+    const int ext_y = (P.N + tile_rows - 1) / tile_rows * tile_rows;
+    const int ext = ext_x > ext_y ? ext_x : ext_y;
     const double m = fmax(P.half - 0.5, ext - 0.5 - P.half);       // max |x_c|, |y_c| of a tile pixel
     const double R = m * 1.4142135623730951;                         // max |rho_c|
     const double f = 0.70710677;

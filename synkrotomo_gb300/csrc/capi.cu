@@ -366,7 +366,7 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         const long long fp_tasks = (long long)q.nslices * q.numrhos * ((q.a + 31) / 32);
         const long long bp_tasks = (long long)q.nslices * ((q.size + 3) / 4) * ((q.size + 31) / 32);
         const long long share = nprob > 1 ? resident_warps / nprob + 1 : resident_warps;
-        h.bp_inrange = bp_windows_in_range(h.P) ? 1 : 0;
+        h.bp_inrange = bp_windows_in_range(h.P, 32) ? 1 : 0;   // BP tiles of 4*(8/bp_split) <= 32 rows
         h.fp_split = q.fp_split ? q.fp_split : pick_fp_split(fp_tasks, share, q.size);
         h.bp_split = q.bp_split ? q.bp_split : pick_bp_split(bp_tasks, share, q.a);
         h.fp_ips = h.bp_ips = 0;

@@ -7,7 +7,9 @@
 //   setup:    setup_kernel     geometry table + angle lists (+ pair images), one launch
 //   forward:  fp_lane_kernel   one warp = one detector x 32 angles of one class
 //             fp_exact_kernel  near-axis angles, the reference's expressions
-//   backward: bp_tile_kernel   one block = 32 x 32 pixels, 4 or 8 per thread, all angles
+//   backward: bp_tile_kernel   one block = 32 x 8*PIX pixels, PIX = 4 or 8 per thread, all angles
+//             bp_split_kernel  the same with the angles split over warps (images too small
+//                              for one block per tile to fill the GPU)
 // See fp_tile.cuh and bp_tile.cuh for the per-ray and per-pixel arithmetic.
 #include <math.h>
 
@@ -482,28 +484,97 @@ __global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_tile_kern
     }
 }
 
-template <int PIX>
-static void launch_bp_pix(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
-                          float *scaled) {
-    dim3 grid((P.N + 31) / 32, (P.N + 8 * PIX - 1) / (8 * PIX));
-    if (scaled) {
-        if (bp_windows_in_range(P)) bp_tile_kernel<PIX, true, true, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
-        else if (P.deltarho == 1.0f)
-            bp_tile_kernel<PIX, true, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
-        else bp_tile_kernel<PIX, false, false, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+// The same pixels with the angles split SB ways (SB = 2, 4, 8), for images
+// whose 32 x 8*PIX tiles are too few to fill the GPU: a block = 8/SB warp
+// rows x SB angle parts, 32 x (8/SB)*PIX pixels; the SB partial sums of a
+// pixel are added in a fixed order through shared memory.
+template <int kBpPix, bool UNIT, bool INRANGE, bool SCALED>
+__global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_split_kernel(ProbGeom P, AngleLists L,
+                                                                    const float *__restrict__ sino_s,
+                                                                    const float *__restrict__ sino,
+                                                                    float *__restrict__ out, int SB) {
+    __shared__ BpStage st;
+    __shared__ float red[8][kBpPix][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int RB = 8 / SB;
+    const int part = warp % SB, wrow = warp / SB;
+    const int col = blockIdx.x * 32 + lane;
+    const int row0 = blockIdx.y * (RB * kBpPix) + wrow;
+    const float xc = (float)(col - P.half) + 0.5f;
+    const float yc0 = (float)(row0 - P.half) + 0.5f;
+    float sum[kBpPix], comp[kBpPix];
+#pragma unroll
+    for (int m = 0; m < kBpPix; ++m) sum[m] = comp[m] = 0.0f;
+    for (int kc = 0; kc < P.a; kc += kBpChunk) {
+        __syncthreads();
+        bp_stage(P, kc, st);
+        __syncthreads();
+        float prt[kBpPix];
+#pragma unroll
+        for (int m = 0; m < kBpPix; ++m) prt[m] = 0.0f;
+        bp_chunk<kBpPix, UNIT, INRANGE, SCALED>(P, st, kc, P.a, part, SB, sino_s, xc, yc0, (float)RB, prt);
+#pragma unroll
+        for (int m = 0; m < kBpPix; ++m) comp_add(sum[m], comp[m], prt[m]);
+    }
+    float ex[kBpPix];
+#pragma unroll
+    for (int m = 0; m < kBpPix; ++m) ex[m] = 0.0f;
+    bp_exact_angles<kBpPix>(P, L.exact, __ldg(L.counts + 2), part, SB, sino, row0, RB, col, ex);
+#pragma unroll
+    for (int m = 0; m < kBpPix; ++m) red[warp][m][lane] = (sum[m] + comp[m]) + ex[m];
+    __syncthreads();
+    if (part != 0) return;
+#pragma unroll
+    for (int m = 0; m < kBpPix; ++m) {
+        float v = red[warp][m][lane];
+        for (int t = 1; t < SB; ++t) v += red[warp + t][m][lane];
+        const int row = row0 + RB * m;
+        if (row < P.N && col < P.N) out[(size_t)row * P.N + col] = v;
+    }
+}
+
+// Angle split of the backprojection: the smallest SB whose tiles give at
+// least four blocks per SM (1 when the unsplit tiles already do), with at
+// least 8 angles per part (a split of a few angles only idles warps).
+static int bp_angle_split(const ProbGeom &P, int pix) {
+    const long long want = 4LL * device_sms();
+    const long long cols = (P.N + 31) / 32;
+    const int maxs = P.a >= 64 ? 8 : (P.a >= 32 ? 4 : (P.a >= 16 ? 2 : 1));
+    int SB = 1;
+    while (SB < maxs && cols * ((P.N + (8 / SB) * pix - 1) / ((8 / SB) * pix)) < want) SB *= 2;
+    return SB;
+}
+
+template <int PIX, bool SCALED>
+static void launch_bp_pix(const ProbGeom &P, const AngleLists &L, const float *sino_s, const float *sino, float *img,
+                          cudaStream_t stream) {
+    const int SB = bp_angle_split(P, PIX);
+    const bool inrange = bp_windows_in_range(P, 8 * PIX);    // split tiles (8/SB)*PIX rows high divide 8*PIX
+    const bool unit = P.deltarho == 1.0f;
+    if (SB == 1) {
+        const dim3 grid((P.N + 31) / 32, (P.N + 8 * PIX - 1) / (8 * PIX));
+        if (inrange) bp_tile_kernel<PIX, true, true, SCALED><<<grid, 256, 0, stream>>>(P, L, sino_s, sino, img);
+        else if (unit) bp_tile_kernel<PIX, true, false, SCALED><<<grid, 256, 0, stream>>>(P, L, sino_s, sino, img);
+        else bp_tile_kernel<PIX, false, false, SCALED><<<grid, 256, 0, stream>>>(P, L, sino_s, sino, img);
     } else {
-        if (bp_windows_in_range(P)) bp_tile_kernel<PIX, true, true, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
-        else if (P.deltarho == 1.0f)
-            bp_tile_kernel<PIX, true, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
-        else bp_tile_kernel<PIX, false, false, false><<<grid, 256, 0, stream>>>(P, L, sino, sino, img);
+        const int th = (8 / SB) * PIX;
+        const dim3 grid((P.N + 31) / 32, (P.N + th - 1) / th);
+        if (inrange) bp_split_kernel<PIX, true, true, SCALED><<<grid, 256, 0, stream>>>(P, L, sino_s, sino, img, SB);
+        else if (unit) bp_split_kernel<PIX, true, false, SCALED><<<grid, 256, 0, stream>>>(P, L, sino_s, sino, img, SB);
+        else bp_split_kernel<PIX, false, false, SCALED><<<grid, 256, 0, stream>>>(P, L, sino_s, sino, img, SB);
     }
 }
 
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
                       float *scaled) {
-    if (scaled) row_scale_kernel<<<dim3((P.D + 255) / 256, P.a), 256, 0, stream>>>(P, sino, scaled);
-    if (P.a >= kBpManyAngles) launch_bp_pix<8>(P, L, sino, img, stream, scaled);
-    else launch_bp_pix<4>(P, L, sino, img, stream, scaled);
+    if (scaled) {
+        row_scale_kernel<<<dim3((P.D + 255) / 256, P.a), 256, 0, stream>>>(P, sino, scaled);
+        if (P.a >= kBpManyAngles) launch_bp_pix<8, true>(P, L, scaled, sino, img, stream);
+        else launch_bp_pix<4, true>(P, L, scaled, sino, img, stream);
+    } else {
+        if (P.a >= kBpManyAngles) launch_bp_pix<8, false>(P, L, sino, sino, img, stream);
+        else launch_bp_pix<4, false>(P, L, sino, sino, img, stream);
+    }
     return cudaGetLastError();
 }
 

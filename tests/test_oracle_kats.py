@@ -145,3 +145,14 @@ def test_cpu_sirt_rejects_odd_sides():
     rhos = np.float32(g.rhozero) + np.arange(g.numrhos, dtype=np.float32)
     with pytest.raises(ValueError):
         cpu_ref.sirt3d(g.angles, rhos, np.zeros(9 * sino.size, np.float32), 2, 9)
+
+
+@pytest.mark.parametrize("size,a,nr", [(32, 20, None), (40, 33, 61)])
+def test_fp64_backprojection_rows_match_the_matrix(size, a, nr):
+    """The row-by-row FP64 backprojection (used where the full matrix would be
+    too large) is the matrix oracle restricted to those rows."""
+    g = phantom.geometry(size, a, numrhos=nr)
+    y = np.random.default_rng(1).random(g.n_rays).astype(np.float32)
+    full = F.backprojection(g.angles, g.rhozero, g.deltarho, size, y).reshape(size, size)
+    rows = [0, 3, size // 2, size - 1]
+    np.testing.assert_array_equal(F.backprojection_rows(g.angles, g.rhozero, g.deltarho, size, y, rows), full[rows])

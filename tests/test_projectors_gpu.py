@@ -147,3 +147,50 @@ def test_many_angles_and_repeated_axis_angles(gpu):
     bt = rt.backprojection(_dev(ang), g.rhozero, 1.0, size, _dev(y)).cpu().numpy()
     ref_bt = cpu_ref.backprojection(ang, g.rhozero, 1.0, size, y)
     assert rel_l2(bt, ref_bt) < TOL
+
+
+@pytest.mark.parametrize("size,a,nr", [
+    (96, 300, 139),      # 8 pixels per thread, N = 32 mod 64, detector window proof just holding
+    (160, 260, None),    # the same with the default detector count
+    (512, 360, 725),     # few 32 x 64 tiles: the angles split over warps
+    (200, 40, None),     # 4 pixels per thread, angles split
+])
+def test_backprojection_tile_shapes(gpu, size, a, nr):
+    g = _geom(size, a, nr, 1.0, math.pi)
+    y = np.random.default_rng(size + a).random(g.n_rays).astype(np.float32)
+    out = rt.backprojection(_dev(g.angles), g.rhozero, g.deltarho, size, _dev(y)).cpu().numpy()
+    ref32 = cpu_ref.backprojection(g.angles, g.rhozero, g.deltarho, size, y)
+    assert rel_l2(out, ref32) < TOL
+    assert np.max(np.abs(out - ref32)) <= 1e-4 * max(1.0, float(np.max(np.abs(ref32))))
+
+
+def test_bench_size_against_oracle_sampled_angles(gpu):
+    """N=2048 with the benchmark's 2897 detectors and every 8th of its 2048
+    angles (256: the 8-pixels-per-thread backprojector).
+
+    The backprojector's trapezoid weights and the reference's intersect_fact
+    are two FP32 formulations of the same lengths; over 256 angles of a
+    2048-wide image their sums differ by ~1.3e-5 rel-L2 (rounding of the
+    detector coordinate |q| ~ 1450, amplified by the 1/b edges of angles next
+    to an axis), so this size states its own bar: 2.5e-5 against the FP32
+    reference, and no less accurate than that reference against the FP64
+    oracle on sampled rows (which it misses by ~3e-3 here: the f32 rounding of
+    edge rays at integer rhozero).  The forward projector keeps the 1e-5 bar."""
+    size, nr = 2048, 2897
+    angles = np.linspace(0.0, math.pi, 2048, endpoint=False).astype(np.float32)[::8].copy()
+    rz = float(np.float32(-(nr - 1) / 2.0))
+    y = np.random.default_rng(8).random(angles.size * nr).astype(np.float32)
+    out = rt.backprojection(_dev(angles), rz, 1.0, size, _dev(y)).cpu().numpy().reshape(size, size)
+    ref = cpu_ref.backprojection(angles, rz, 1.0, size, y).reshape(size, size)
+    assert rel_l2(out, ref) < 2.5e-5
+    # worst of 4.2M pixels: 2.1e-4 of the maximum measured (the FP32 reference
+    # itself is up to 6e-3 of the maximum away from FP64 on the sampled rows)
+    assert np.max(np.abs(out - ref)) <= 5e-4 * float(np.max(np.abs(ref)))
+    rows = [0, 1, 2, 3, 1023, 1024, 2046, 2047]
+    r64 = F.backprojection_rows(angles, rz, 1.0, size, y, rows)
+    assert rel_l2(out[rows], r64) <= 1.01 * rel_l2(ref[rows], r64)
+    img = phantom.ellipse_phantom(size, seed=12)
+    fp = rt.forwardprojection(_dev(angles), rz, 1.0, nr, _dev(img)).cpu().numpy()
+    fref = cpu_ref.forwardprojection(angles, rz, 1.0, nr, img)
+    assert rel_l2(fp, fref) < TOL
+    assert np.max(np.abs(fp - fref)) <= 1e-4 * max(1.0, float(np.max(np.abs(fref))))
