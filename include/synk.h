@@ -117,10 +117,10 @@ typedef struct synk_sirt_options {
     int32_t fp_split;
     int32_t bp_split;
     /* Engine and grid: > 0 = the persistent kernel with that many blocks;
-     * 0 = automatic (one launch per phase and iteration when an iteration is
-     * small: at most 6e7 ray-row steps plus pixel-angle pairs, e.g. a few
-     * slices of N <= 256; otherwise the persistent kernel with every block
-     * that fits); -1 = one launch per phase and iteration. */
+     * 0 = automatic (one launch per phase and iteration for a single problem,
+     * and for batches whose iteration is small: at most 6e7 ray-row steps plus
+     * pixel-angle pairs; otherwise the persistent kernel with every block that
+     * fits); -1 = one launch per phase and iteration. */
     int32_t grid_blocks;
 } synk_sirt_options;
 

@@ -268,12 +268,16 @@ int valid_split(int s) { return s == 1 || s == 2 || s == 4 || s == 8; }
 // `staging`: optional pinned host buffer of nprob SirtProblem entries; the
 // problem table is uploaded from it (a copy a CUDA graph can capture) instead
 // of from pageable memory.
-// Per-iteration work (FP ray-row steps + BP pixel-angle pairs) up to which the
-// phase-split engine replaces the persistent kernel.  Measured on GB300: at
-// N=128 / 1-8 slices and N=256 / 1 slice the two launches per iteration cost
-// less than the persistent kernel's two grid barriers (1.17-1.32x faster);
-// from about 8e7 on the engines are within a few percent of each other.
-constexpr double kSplitMaxWork = 6.0e7;
+// Engine choice by the work per iteration (FP ray-row steps + BP pixel-angle
+// pairs), measured on GB300 with both engines forced on the same inputs:
+// - up to kSmallWork the phase-split engine with the generic forward phase
+//   (two launches per iteration, no grid barrier) beats the persistent kernel
+//   1.08-1.32x (N=64-256, 1-64 slices);
+// - above it, for one problem, the split engine whose forward phase runs on
+//   the projector's own grid beats it 1.04-1.16x (N=256-1024, 1-256 slices;
+//   N=2048 / 1 slice even); batches of several problems keep the persistent
+//   kernel there.
+constexpr double kSmallWork = 6.0e7;
 
 int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double tol, int grid_blocks,
                void *staging = nullptr) {
@@ -413,21 +417,25 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
     sp.tol2 = tol > 0.0 ? tol * tol : 0.0;
     sp.record_final = want_res ? 1 : 0;
     sp.dynamic = nprob > 1 ? 1 : 0;
-    // Engine: one launch per phase and iteration for small iterations, the
-    // fused persistent kernel otherwise (grid_blocks == -1 forces the split
-    // engine, > 0 the persistent kernel; 0 decides by the work per iteration).
+    // Engine: one launch per phase and iteration (single problems, and small
+    // batches), the fused persistent kernel otherwise (grid_blocks == -1
+    // forces the split engine, > 0 the persistent kernel; 0 decides).
     double work = 0.0;   // FP ray-row steps + BP (pixel, angle) pairs per iteration
     for (int i = 0; i < nprob; ++i)
         work += (double)in[i].nslices * (double)in[i].a * in[i].size * ((double)in[i].size + in[i].numrhos);
     // (a captured plan keeps the persistent kernel unless forced: it cannot end the loop early)
-    const bool split = grid_blocks == -1 || (grid_blocks == 0 && !staging && work <= kSplitMaxWork);
+    const bool split = grid_blocks == -1 || (grid_blocks == 0 && !staging && (nprob == 1 || work <= kSmallWork));
     if (split) {
         int fpg = 0, bpg = 0;
         if (!sirt_phase_grids(&fpg, &bpg)) return fail(ctx, SYNK_ECUDA, "SIRT phase kernels cannot be resident");
         sp.dynamic = 0;
         int *active = reinterpret_cast<int *>(words + 7);
+        // one large problem: the forward phase on the projector's own grid
+        const bool stack = nprob == 1 && work > kSmallWork && host[0].nslices <= 65535 &&
+                           (host[0].P.a + 31) / 32 + 2 <= 65535;
         for (int it = 0; it <= max_iter; ++it) {
-            SYNK_CUDA(launch_sirt_fp_phase(sp, it, fpg, st), "SIRT forward phase");
+            if (stack) SYNK_CUDA(launch_sirt_fp_stack(host[0], it, sp.tol2, sp.record_final, st), "SIRT forward phase");
+            else SYNK_CUDA(launch_sirt_fp_phase(sp, it, fpg, st), "SIRT forward phase");
             if (it == max_iter) break;
             SYNK_CUDA(launch_sirt_bp_phase(sp, it, active, bpg, st), "SIRT backward phase");
             // every 16 iterations, end the loop once no slice updates any more

@@ -331,6 +331,77 @@ __global__ void __launch_bounds__(256, 5) sirt_fp_phase_kernel(SirtParams p, int
     fp_phase(p, it, nullptr, sh);
 }
 
+// Forward phase of the split engine for a single problem (a stack of slices):
+// the standalone projector's grid (8/S detectors x S row parts per block, one
+// angle group per blockIdx.y, one slice per blockIdx.z) with the residual as
+// its epilogue.  Without the phase functions' item bookkeeping it keeps the
+// projector's register count and occupancy; the per-ray values are those of
+// fp_phase (same rows, same split, same order), so the iterates are the same.
+template <int S>
+__global__ void __launch_bounds__(256) sirt_fp_stack_kernel(SirtProblem q, int it, double tol2, int record_final) {
+    __shared__ float red[8][32];
+    __shared__ double e2s;
+    const int s = blockIdx.z;
+    if (it > q.iterations || (it == q.iterations && !record_final)) return;       // block-uniform
+    if (tol2 > 0.0 && stop_of(q, s) < it) return;
+    const int grp = blockIdx.y;
+    const int nsteep = __ldg(q.L.counts), nflat = __ldg(q.L.counts + 1);
+    if (grp >= nsteep + nflat) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) e2s = 0.0;
+    const int part = warp % S;
+    const int r = blockIdx.x * (8 / S) + warp / S;
+    const int rr = r < q.P.D ? r : q.P.D - 1;
+    const int k = __ldg(q.L.order + grp * 32 + lane);
+    const int jb = (int)((long long)part * q.P.N / S), je = (int)((long long)(part + 1) * q.P.N / S);
+    const size_t np = (size_t)q.P.N * (q.P.N + 2);
+    const float *img = (grp < nsteep ? q.xpad : q.xTpad) + (size_t)s * np;
+    const int kk = r < q.P.D ? k : -1;
+    const float v = fp_lane_ray(q.P, kk, rr, img, jb, je);
+    red[warp][lane] = v;
+    __syncthreads();
+    double e2 = 0.0;
+    if (part == 0 && kk >= 0) {
+        float fpv = red[warp][lane];
+        for (int t = 1; t < S; ++t) fpv += red[warp + t][lane];
+        e2 = residual(q, s, kk, r, fpv);
+    }
+    e2 = warp_sum_d(e2);
+    if (lane == 0 && e2 != 0.0) atomicAdd(&e2s, e2);
+    __syncthreads();
+    if (threadIdx.x == 0 && e2s != 0.0) atomicAdd(q.res2 + (size_t)s * (q.iterations + 1) + it, e2s);
+}
+
+// Near-axis rays of the same phase: a warp per ray (8 detectors per block),
+// kExactSlotsSirt angle slots, one slice per blockIdx.z.
+constexpr int kExactSlotsSirt = 4;
+
+__global__ void __launch_bounds__(256) sirt_fp_stack_exact_kernel(SirtProblem q, int it, double tol2,
+                                                                  int record_final) {
+    __shared__ double e2s;
+    const int s = blockIdx.z;
+    if (it > q.iterations || (it == q.iterations && !record_final)) return;
+    if (tol2 > 0.0 && stop_of(q, s) < it) return;
+    const int nexact = __ldg(q.L.counts + 2);
+    if ((int)blockIdx.y >= nexact) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) e2s = 0.0;
+    __syncthreads();
+    const int r = blockIdx.x * 8 + warp;
+    const size_t np = (size_t)q.P.N * (q.P.N + 2);
+    double e2 = 0.0;
+    for (int e = blockIdx.y; e < nexact; e += gridDim.y) {
+        const int k = __ldg(q.L.exact + e);
+        if (r < q.P.D) {                                   // warp-uniform
+            const float v = fp_exact_ray_warp(q.P, k, r, q.xpad + (size_t)s * np, q.xTpad + (size_t)s * np);
+            if (lane == 0) e2 += residual(q, s, k, r, v);
+        }
+    }
+    if (lane == 0 && e2 != 0.0) atomicAdd(&e2s, e2);
+    __syncthreads();
+    if (threadIdx.x == 0 && e2s != 0.0) atomicAdd(q.res2 + (size_t)s * (q.iterations + 1) + it, e2s);
+}
+
 // Block 0 also applies the stopping rule of iteration it (the same decision
 // as the fused kernel: every block's bp_needed reads the same residuals) and
 // stores the number of slices still updating in *active.
@@ -451,6 +522,23 @@ int sirt_phase_grids(int *fp_grid, int *bp_grid) {
 
 cudaError_t launch_sirt_fp_phase(const SirtParams &p, int it, int grid, cudaStream_t stream) {
     sirt_fp_phase_kernel<<<grid, 256, 0, stream>>>(p, it);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sirt_fp_stack(const SirtProblem &q, int it, double tol2, int record_final, cudaStream_t stream) {
+    const int S = q.fp_split;
+    const int gmax = (q.P.a + 31) / 32 + 2;
+    const dim3 grid((q.P.D + 8 / S - 1) / (8 / S), gmax, q.nslices);
+    switch (S) {
+        case 1: sirt_fp_stack_kernel<1><<<grid, 256, 0, stream>>>(q, it, tol2, record_final); break;
+        case 2: sirt_fp_stack_kernel<2><<<grid, 256, 0, stream>>>(q, it, tol2, record_final); break;
+        case 4: sirt_fp_stack_kernel<4><<<grid, 256, 0, stream>>>(q, it, tol2, record_final); break;
+        default: sirt_fp_stack_kernel<8><<<grid, 256, 0, stream>>>(q, it, tol2, record_final); break;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const dim3 ge((q.P.D + 7) / 8, kExactSlotsSirt, q.nslices);
+    sirt_fp_stack_exact_kernel<<<ge, 256, 0, stream>>>(q, it, tol2, record_final);
     return cudaGetLastError();
 }
 

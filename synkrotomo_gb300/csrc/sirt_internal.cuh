@@ -55,6 +55,8 @@ cudaError_t launch_sirt_persistent(const SirtParams &p, int grid, cudaStream_t s
 int sirt_phase_grids(int *fp_grid, int *bp_grid);
 cudaError_t launch_sirt_fp_phase(const SirtParams &p, int it, int grid, cudaStream_t stream);
 cudaError_t launch_sirt_bp_phase(const SirtParams &p, int it, int *active, int grid, cudaStream_t stream);
+// forward phase of the split engine for one problem (a slice stack): the projector's grid, residual epilogue
+cudaError_t launch_sirt_fp_stack(const SirtProblem &q, int it, double tol2, int record_final, cudaStream_t stream);
 cudaError_t launch_sirt_finalize(SirtProblem *probs, int nprob, int max_slices, int record_final,
                                  cudaStream_t stream);
 

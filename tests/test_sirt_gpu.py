@@ -162,3 +162,24 @@ def test_phase_split_engine_uneven_batch(gpu):
         assert int(p.done.item()) == spec[2]
     with pytest.raises(ValueError):
         rt.sirt_batch(probs, grid_blocks=-2)
+
+
+def test_phase_split_engine_large_stack_matches_persistent(gpu):
+    """Above 6e7 work per iteration a single problem's forward phase runs on the
+    projector's grid (sirt_fp_stack_kernel): the same per-ray values, so the
+    iterates equal the persistent kernel's bit for bit."""
+    size, a, ns, its = 256, 180, 4, 12
+    g = phantom.geometry(size, a)
+    vol = phantom.ellipsoid_volume(size, ns, seed=5)
+    sinos = np.stack([cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, g.numrhos, vol[i])
+                      for i in range(ns)])
+    ang, bd = _dev(g.angles), _dev(sinos.ravel())
+    assert ns * a * size * (size + g.numrhos) > 6e7
+    xp, rp, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
+                               grid_blocks=rt.resident_blocks())
+    xs, rs, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
+                               grid_blocks=-1)
+    assert torch.equal(xp, xs)
+    np.testing.assert_allclose(rs.cpu().numpy(), rp.cpu().numpy(), rtol=1e-12)
+    ref = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), sinos[1], its)
+    assert rel_l2(xs.cpu().numpy().reshape(ns, -1)[1], ref) < 1e-5
