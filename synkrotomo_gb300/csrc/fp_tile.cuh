@@ -1,13 +1,17 @@
 // Ray-driven forward projection with one lane per angle, shared by the
-// standalone forward projector and the persistent SIRT kernel.
+// standalone forward projector and the SIRT kernels.
 //
 // A warp owns one detector index r and 32 angles of the same class (all steep
 // or all flat, none near-axis).  The 32 rays of neighbouring angles at the
-// same detector cross almost the same pixels of a frame row, so each of the
-// warp's two gathers per row touches 2-3 sectors (lanes on adjacent detectors
-// of one angle would span ~45 columns).  Images are read from a padded copy
-// (row stride N+2, a zero column on each side) so one predicate covers both
-// pixels of a row segment.  Per lane and row (forwardprojection.fut:31-56):
+// same detector cross almost the same pixels of a frame row, so each gather of
+// a row touches 2-3 sectors (lanes on adjacent detectors of one angle would
+// span ~45 columns).  Two image layouts:
+//   fp_lane_ray_pair (standalone projector): pair images, entry i of a row =
+//     (pixel i-1, pixel i - pixel i-1) with zeros outside the image and a zero
+//     entry ending the row; one unconditional 8-byte gather per row step.
+//   fp_lane_ray (SIRT, whose iterate is kept padded): row stride N+2, a zero
+//     column on each side, so one predicate covers both 4-byte gathers.
+// Per lane and row (forwardprojection.fut:31-56):
 //   u  = j*slope + u0                  left end of the row segment, pixel units
 //   c  = floor(u), t = max(0, (u - c + |slope| - 1) / |slope|)   share of c+1
 //   s += v[c] + t*(v[c+1] - v[c])      (times lbase once per ray)
