@@ -1,7 +1,7 @@
-// Persistent SIRT kernel (futhark/SIRT.fut:27-39 per slice; futhark/SIRT3D.fut:
-// 23-28 for slice stacks; any number of independent problems of uneven size).
+// SIRT engines (futhark/SIRT.fut:27-39 per slice; futhark/SIRT3D.fut:23-28 for
+// slice stacks; any number of independent problems of uneven size).
 //
-// One cooperative launch runs every iteration of every problem:
+// Persistent engine: one cooperative launch runs every iteration of every problem:
 //   phase FP (iteration k):  e = b - FP(x_k), rr = R*e, sum e^2 (FP64)
 //   grid barrier
 //   phase BP (iteration k):  x_{k+1} = x_k + C*BP(rr), written to the padded
@@ -17,6 +17,11 @@
 // spins with a time limit; a block that gives up records SYNK_ETIMEOUT in the
 // status word and returns, after which every other block gives up at its next
 // barrier too.
+//
+// The phase-split engine runs the same phases as ordinary launches, one per
+// phase and iteration (the kernel boundary replaces the barrier); for a single
+// problem its forward phase runs on the projector's own grid
+// (sirt_fp_stack_kernel).  The host picks the engine (capi.cu, sirt_batch).
 #include <limits.h>
 #include <math.h>
 
