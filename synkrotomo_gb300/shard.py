@@ -12,7 +12,8 @@ gathered at the end. No collective runs on the data path.
   row-steps of the forward projector plus the pixel-angle pairs of the
   backprojector.
 * ``gather_items``: every rank gets every rank's results (one all-gather of
-  padded flat buffers, after one all-reduce of the lengths).
+  padded flat buffers, after a check that all ranks hold the same assignment
+  and one all-reduce of the lengths).
 * ``sirt3d_sharded`` / ``batch_sharded``: the two drivers.
 * ``max_over_ranks``: the timing reduction of a weak-scaling run.
 
@@ -23,6 +24,7 @@ same one without talking to the others.
 from __future__ import annotations
 
 import heapq
+import zlib
 from typing import Callable, Dict, List, Sequence, Tuple
 
 import numpy as np
@@ -124,6 +126,13 @@ def gather_items(local: Dict[int, torch.Tensor], owner: Sequence[int], group=Non
         return [local[i].reshape(-1) for i in range(n)]
     d = _dist()
     dev = _comm_device(group)
+    # every rank must hold the same assignment (it is computed, not exchanged):
+    # compare a checksum with one min/max reduction, and raise on every rank alike
+    sig = float(zlib.crc32(np.asarray(owner, dtype=np.int64).tobytes())) + 2.0 ** 32 * n
+    chk = torch.tensor([sig, -sig], dtype=torch.float64, device=dev)
+    d.all_reduce(chk, op=d.ReduceOp.MAX, group=group)
+    if chk[0].item() != -chk[1].item():
+        raise ValueError("the ranks hold different item assignments (different costs or item counts)")
     lens = torch.zeros(max(n, 1), dtype=torch.int64, device=dev)
     for i, t in local.items():
         lens[i] = t.numel()

@@ -162,3 +162,39 @@ def test_two_gloo_ranks_match_single_process():
             np.testing.assert_array_equal(a, b)
         assert sorted(set(owner)) == [0, 1]          # both ranks got work
     assert got[0][3] == got[1][3]                    # same assignment on every rank
+
+
+def _mismatch_worker(rank, world, port, q):
+    import torch.distributed as dist
+    try:
+        dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+        costs = [3.0, 1.0, 2.0] if rank == 0 else [3.0, 1.0, 2.0, 5.0]    # rank 1 sees another batch
+        try:
+            shard.batch_sharded(costs, lambda idx: [torch.zeros(2) for _ in idx])
+            q.put((rank, "no error"))
+        except ValueError as e:
+            q.put((rank, "ValueError"))
+        dist.destroy_process_group()
+    except Exception as e:
+        q.put((rank, repr(e)))
+
+
+def test_ranks_with_different_assignments_fail_together():
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_mismatch_worker, args=(k, world, port, q)) for k in range(world)]
+    for p in procs:
+        p.start()
+    got = {}
+    try:
+        for _ in range(world):
+            rank, what = q.get(timeout=240)
+            got[rank] = what
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.is_alive():
+                p.kill()
+    assert got == {0: "ValueError", 1: "ValueError"}
