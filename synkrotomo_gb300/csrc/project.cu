@@ -6,6 +6,7 @@
 //
 //   setup:    setup_kernel     geometry table + angle lists (+ pair images), one launch
 //   forward:  fp_lane_kernel   one warp = one detector x 32 angles of one class
+//             fp_det_kernel    fewer than 32 angles: one warp = 32 detectors of one angle
 //             fp_exact_kernel  near-axis angles, the reference's expressions
 //   backward: bp_tile_kernel   one block = 32 x 8*PIX pixels, PIX = 4 or 8 per thread, all angles
 //             bp_split_kernel  the same with the angles split over warps (images too small
@@ -359,6 +360,36 @@ __global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, 
     if (k >= 0 && r < P.D) sino[(size_t)k * P.D + r] = v;
 }
 
+// Fewer than 32 angles (sparse-view data): one warp = 32 consecutive detectors
+// of one angle, so no lane idles, and a block of 32 warps splits each ray into
+// S row parts (S up to 32, at least 16 rows a part) so that each warp's chain
+// of dependent gathers is short.  The per-ray arithmetic is fp_lane_kernel's
+// (fp_lane_ray_pair); the S partial sums are added in a fixed order.
+template <int S>
+__global__ void __launch_bounds__(1024) fp_det_kernel(ProbGeom P, AngleLists L, const float2 *__restrict__ xpair,
+                                                      const float2 *__restrict__ xTpair, float *__restrict__ sino) {
+    __shared__ float red[32][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int steep_slots = __ldg(L.counts) * 32;
+    const int nslots = steep_slots + __ldg(L.counts + 1) * 32;
+    const int slot = blockIdx.y;
+    if (slot >= nslots) return;                       // block-uniform
+    const int k = __ldg(L.order + slot);
+    if (k < 0) return;                                // block-uniform: padding of a group
+    const int part = warp % S;
+    const int r = (blockIdx.x * (32 / S) + warp / S) * 32 + lane;
+    const int jb = part * P.N / S, je = (part + 1) * P.N / S;
+    const bool in = r < P.D;
+    float v = fp_lane_ray_pair(P, in ? k : -1, in ? r : P.D - 1, slot < steep_slots ? xpair : xTpair, jb, je);
+    if (S > 1) {
+        red[warp][lane] = v;
+        __syncthreads();
+        if (part != 0) return;
+        for (int t = 1; t < S; ++t) v += red[warp + t][lane];
+    }
+    if (in) sino[(size_t)k * P.D + r] = v;
+}
+
 // Near-axis rays (the reference's own expressions, on the pair images' first
 // halves): a warp per (ray, row part), 8/S rays per block, kExactSlots angle
 // slots (at most four near-axis angles lie in [0, 2 pi); repeats loop).
@@ -399,15 +430,31 @@ static int fp_row_split(long long warps) {
 
 cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float2 *xpair, const float2 *xTpair, float *sino,
                       cudaStream_t stream) {
-    // groups of 32 angles: at most ceil(a/32) + 2 (the steep/flat split adds one partial group each)
-    const int gmax = (P.a + 31) / 32 + 2;
-    const int S = fp_row_split((long long)((P.a + 31) / 32) * P.D);
-    const dim3 grid((P.D + 8 / S - 1) / (8 / S), gmax);
-    switch (S) {
-        case 1: fp_lane_kernel<1><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
-        case 2: fp_lane_kernel<2><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
-        case 4: fp_lane_kernel<4><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
-        default: fp_lane_kernel<8><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+    if (P.a < 32) {
+        // at most one group of each class: 64 angle slots; rows split to >= 16 a part
+        int S = 1;
+        while (S < 32 && P.N / (2 * S) >= 16) S *= 2;
+        const int dgroups = (P.D + 31) / 32;
+        const dim3 grid((dgroups + 32 / S - 1) / (32 / S), 64);
+        switch (S) {
+            case 1: fp_det_kernel<1><<<grid, 1024, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            case 2: fp_det_kernel<2><<<grid, 1024, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            case 4: fp_det_kernel<4><<<grid, 1024, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            case 8: fp_det_kernel<8><<<grid, 1024, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            case 16: fp_det_kernel<16><<<grid, 1024, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            default: fp_det_kernel<32><<<grid, 1024, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        }
+    } else {
+        // groups of 32 angles: at most ceil(a/32) + 2 (the steep/flat split adds one partial group each)
+        const int gmax = (P.a + 31) / 32 + 2;
+        const int S = fp_row_split((long long)((P.a + 31) / 32) * P.D);
+        const dim3 grid((P.D + 8 / S - 1) / (8 / S), gmax);
+        switch (S) {
+            case 1: fp_lane_kernel<1><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            case 2: fp_lane_kernel<2><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            case 4: fp_lane_kernel<4><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+            default: fp_lane_kernel<8><<<grid, 256, 0, stream>>>(P, L, xpair, xTpair, sino); break;
+        }
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
