@@ -120,7 +120,11 @@ typedef struct synk_sirt_options {
      * 0 = automatic (one launch per phase and iteration for a single problem,
      * and for batches whose iteration is small: at most 6e7 ray-row steps plus
      * pixel-angle pairs; otherwise the persistent kernel with every block that
-     * fits); -1 = one launch per phase and iteration. */
+     * fits); -1 = one launch per phase and iteration.  With tol > 0 the
+     * launch loop ends early: every 16 iterations the call reads the number of
+     * slices still updating, which waits for the stream (not while the stream
+     * is being captured into a graph; the loop then runs to the end, each
+     * launch doing nothing once every slice has stopped). */
     int32_t grid_blocks;
 } synk_sirt_options;
 

@@ -430,6 +430,11 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         if (!sirt_phase_grids(&fpg, &bpg)) return fail(ctx, SYNK_ECUDA, "SIRT phase kernels cannot be resident");
         sp.dynamic = 0;
         int *active = reinterpret_cast<int *>(words + 7);
+        // the early exit reads the active count on the host: not inside a graph
+        // capture (the library's own plan, or a caller capturing this stream)
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusNone;
+        const bool can_poll = sp.tol2 > 0.0 && !staging && cap == cudaStreamCaptureStatusNone;
         // one large problem: the forward phase on the projector's own grid
         const bool stack = nprob == 1 && work > kSmallWork && host[0].nslices <= 65535 &&
                            (host[0].P.a + 31) / 32 + 2 <= 65535;
@@ -439,8 +444,7 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
             if (it == max_iter) break;
             SYNK_CUDA(launch_sirt_bp_phase(sp, it, active, bpg, st), "SIRT backward phase");
             // every 16 iterations, end the loop once no slice updates any more
-            // (not while a graph is being captured: no host reads there)
-            if (sp.tol2 > 0.0 && !staging && (it & 15) == 15) {
+            if (can_poll && (it & 15) == 15) {
                 int h_active = 1;
                 SYNK_CUDA(cudaMemcpyAsync(&h_active, active, sizeof(int), cudaMemcpyDeviceToHost, st), "read active");
                 SYNK_CUDA(cudaStreamSynchronize(st), "read active");
