@@ -39,3 +39,34 @@ def test_reference_arm_other_ranks_print_nothing():
     r = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert r.returncode == 0, r.stderr[-2000:]
     assert not [l for l in r.stdout.splitlines() if l.startswith("{")]
+
+
+def _bench_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_clock_summary_reads_the_samples_of_the_timed_region():
+    bench = _bench_module()
+    cs = bench.ClockSampler()
+    # index, clocks.sm, clocks.max.sm, power, active mask, hw, hw_thermal, sw_thermal, sw_power_cap
+    before = "0, 1200, 2070, 300.0, 0x0, Not Active, Not Active, Not Active, Not Active"
+    inside = ["0, 2070, 2070, 900.5, 0x0, Not Active, Not Active, Not Active, Not Active",
+              "0, 2040, 2070, 1350.0, 0x4, Not Active, Not Active, Not Active, Active",
+              "0, 2055, 2070, 1100.0, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    cs.lines = [before] + inside
+    cs.start = 1
+    s = cs.summary()
+    assert s["sm_mhz"] == 2055.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
+    assert s["reasons"] == ["sw_power_cap"]
+    cs.lines = [before, "0, 1900, 2070, 1300.0, 0x40, Not Active, Active, Not Active, Not Active"]
+    cs.start = 1
+    assert cs.summary()["reasons"] == ["hw_thermal_slowdown"]
+    # a region too short for a sample: the last one before its end
+    cs.lines, cs.start = [before], 1
+    assert cs.summary()["sm_mhz"] == 1200.0
+    cs.lines, cs.start = [], 0
+    assert cs.summary()["reasons"] == ["unsampled"]
