@@ -97,18 +97,21 @@ class SIRT(_Entry):
 
 class SIRT3D(_Entry):
     """futhark/SIRT3D.fut:18-29 (intended semantics: rhozero = rhos[0],
-    deltarho = rhos[1] - rhos[0], ``size`` slices from a zero start)."""
+    deltarho = rhos[1] - rhos[0], ``size`` slices from a zero start).  The
+    keyword ``nslices`` (no reference counterpart) reconstructs a stack of
+    that many size x size slices instead of ``size``."""
 
     entry_points = {"main": (["[]f32", "[]f32", "[]f32", "i32", "i32"], ["[]f32"])}
 
-    def main(self, angles, rhos, projections, iterations, size):
+    def main(self, angles, rhos, projections, iterations, size, nslices=None):
         with torch.cuda.device(self.device):
             a = rt.to_device_f32(angles, 0, "angles", self.device)
             rh = rt.to_device_f32(rhos, 1, "rhos", self.device)
             proj = rt.to_device_f32(projections, 2, "projections", self.device)
             its = rt.scalar_i32(iterations, 3, "iterations")
             sz = rt.scalar_i32(size, 4, "size")
-            out = rt.sirt3d(a, rh, proj, its, sz)
+            ns = None if nslices is None else rt.scalar_i32(nslices, 5, "nslices")
+            out = rt.sirt3d(a, rh, proj, its, sz, nslices=ns)
             return self._wrap(out)
 
 

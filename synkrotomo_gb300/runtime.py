@@ -322,8 +322,25 @@ def sirt(angles: torch.Tensor, rhozero: float, deltarho: float, image: torch.Ten
 
 
 def sirt3d(angles: torch.Tensor, rhos: torch.Tensor, projections: torch.Tensor, iterations: int, size: int,
-           out: torch.Tensor | None = None) -> torch.Tensor:
-    """``size`` slices reconstructed independently (futhark/SIRT3D.fut:18-29)."""
+           out: torch.Tensor | None = None, nslices: int | None = None) -> torch.Tensor:
+    """``size`` slices reconstructed independently (futhark/SIRT3D.fut:18-29),
+    with rhozero = rhos[0] and deltarho = rhos[1] - rhos[0] (float32).
+
+    ``nslices``: a stack of that many ``size`` x ``size`` slices instead of
+    ``size`` (projections then hold nslices*a*len(rhos) values)."""
+    if nslices is not None:
+        ns, r = int(nslices), rhos.numel()
+        if ns < 1:
+            raise ValueError(f"nslices must be positive (got {ns})")
+        if r < 2:
+            raise ValueError(f"rhos needs at least two detector positions (got {r})")
+        if projections.numel() != ns * angles.numel() * r:
+            raise ValueError(f"projections has {projections.numel()} values, expected nslices*a*r = "
+                             f"{ns * angles.numel() * r}")
+        rh = rhos[:2].detach().cpu().numpy().astype(np.float32)
+        deltarho = float(np.float32(rh[1]) - np.float32(rh[0]))
+        x, _, _ = sirt_slices(angles, float(rh[0]), deltarho, r, size, ns, None, projections, iterations, out=out)
+        return x
     ctx = context(projections.device.index)
     if out is None:
         out = torch.empty(int(size) ** 3, dtype=torch.float32, device=projections.device)

@@ -47,6 +47,21 @@ def test_all_modules(gpu):
     assert rel_l2(v, cpu_ref.sirt3d(g8.angles, rhos, proj, 3, size)) < 1e-5
 
 
+def test_sirt3d_nslices_keyword(gpu):
+    """A non-cubic stack: nslices slices of size x size (keyword without a
+    reference counterpart), the same per-slice SIRT as the cubic call."""
+    from futhark import SIRT3D
+    size, a, ns, nr = 16, 10, 3, 24
+    g = phantom.geometry(size, a, numrhos=nr)
+    rhos = (g.rhozero + np.arange(nr)).astype(np.float32)
+    proj = np.random.default_rng(4).random(ns * a * nr).astype(np.float32)
+    v = SIRT3D.SIRT3D().main(g.angles, rhos, proj, 5, size, nslices=ns).get()
+    assert v.shape == (ns * size * size,)
+    assert rel_l2(v, cpu_ref.sirt3d(g.angles, rhos, proj, 5, size, nslices=ns)) < 1e-5
+    with pytest.raises(ValueError):
+        SIRT3D.SIRT3D().main(g.angles, rhos, proj, 5, size, nslices=ns + 1)
+
+
 def test_argument_errors(gpu):
     from futhark import SIRT, backprojection, forwardprojection
     g = phantom.geometry(16, 4)

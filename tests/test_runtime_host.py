@@ -1,0 +1,30 @@
+"""Host-side argument handling of the runtime (CPU only: the library call is
+replaced by a recorder)."""
+import numpy as np
+import pytest
+import torch
+
+from synkrotomo_gb300 import runtime as rt
+
+
+def test_sirt3d_nslices_passes_the_stack_geometry(monkeypatch):
+    seen = {}
+
+    def record(angles, rhozero, deltarho, numrhos, size, nslices, image, projections, iterations, out=None, **kw):
+        seen.update(rhozero=rhozero, deltarho=deltarho, numrhos=numrhos, size=size, nslices=nslices, image=image,
+                    values=projections.numel(), iterations=iterations)
+        return torch.zeros(nslices * size * size), None, None
+
+    monkeypatch.setattr(rt, "sirt_slices", record)
+    ang = torch.zeros(10)
+    rhos = torch.from_numpy(np.float32(-11.5) + np.arange(24, dtype=np.float32))
+    x = rt.sirt3d(ang, rhos, torch.zeros(3 * 10 * 24), 5, 16, nslices=3)
+    assert x.shape == (3 * 16 * 16,)
+    assert seen == dict(rhozero=-11.5, deltarho=1.0, numrhos=24, size=16, nslices=3, image=None, values=720,
+                        iterations=5)
+    with pytest.raises(ValueError):
+        rt.sirt3d(ang, rhos, torch.zeros(3 * 10 * 24), 5, 16, nslices=0)
+    with pytest.raises(ValueError):
+        rt.sirt3d(ang, rhos, torch.zeros(3 * 10 * 24), 5, 16, nslices=4)     # stack length mismatch
+    with pytest.raises(ValueError):
+        rt.sirt3d(ang, rhos[:1], torch.zeros(30), 5, 16, nslices=3)          # one detector position
