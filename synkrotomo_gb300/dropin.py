@@ -9,10 +9,34 @@ flattened layouts, and run on libsynk instead of OpenCL.
 """
 from __future__ import annotations
 
+import math
+import warnings
+
 import numpy as np
 import torch
 
 from . import runtime as rt
+
+
+class DetectorCoverageWarning(UserWarning):
+    """The detector row is narrower than the image diagonal."""
+
+
+def check_detector_coverage(numrhos: int, deltarho: float, size: int, program: str) -> bool:
+    """Warn when the detector row (numrhos * deltarho) is narrower than the
+    image diagonal, ceil(size * sqrt(2)).  A pixel's detector window can then
+    leave the row: here such detectors contribute 0, where the reference reads
+    the sinogram out of range (backprojection.fut:64).  Returns whether it
+    warned; invalid arguments are left to the library's checks."""
+    if size <= 0 or numrhos <= 0 or not deltarho > 0:
+        return False
+    need = math.ceil(size * math.sqrt(2.0))
+    if numrhos * deltarho < need:
+        warnings.warn(f"{program}: the detector row ({numrhos} detectors x {deltarho}) is narrower than the "
+                      f"image diagonal (ceil({size}*sqrt(2)) = {need}); detectors outside it contribute 0 "
+                      "(the reference reads out of range there)", DetectorCoverageWarning, stacklevel=3)
+        return True
+    return False
 
 
 class _Entry:
@@ -68,6 +92,8 @@ class backprojection(_Entry):
             dr = rt.scalar_f32(deltarho, 2, "deltarho")
             sz = rt.scalar_i32(size, 3, "size")
             proj = rt.to_device_f32(projections, 4, "projections", self.device)
+            if a.numel():
+                check_detector_coverage(proj.numel() // a.numel(), dr, sz, type(self).__name__)
             out = rt.backprojection(a, rz, dr, sz, proj, sparse=self._sparse)
             return self._wrap(out)
 
@@ -91,6 +117,8 @@ class SIRT(_Entry):
             img = rt.to_device_f32(image, 3, "image", self.device)
             proj = rt.to_device_f32(projections, 4, "projections", self.device)
             its = rt.scalar_i32(iterations, 5, "iterations")
+            if a.numel():
+                check_detector_coverage(proj.numel() // a.numel(), dr, math.isqrt(img.numel()), "SIRT")
             out = rt.sirt(a, rz, dr, img, proj, its)
             return self._wrap(out)
 

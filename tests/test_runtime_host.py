@@ -28,3 +28,17 @@ def test_sirt3d_nslices_passes_the_stack_geometry(monkeypatch):
         rt.sirt3d(ang, rhos, torch.zeros(3 * 10 * 24), 5, 16, nslices=4)     # stack length mismatch
     with pytest.raises(ValueError):
         rt.sirt3d(ang, rhos[:1], torch.zeros(30), 5, 16, nslices=3)          # one detector position
+
+
+def test_detector_coverage_warning():
+    import warnings as w
+    from synkrotomo_gb300 import dropin
+    with pytest.warns(dropin.DetectorCoverageWarning):
+        assert dropin.check_detector_coverage(30, 1.0, 48, "backprojection")      # 30 < ceil(48*sqrt 2) = 68
+    with pytest.warns(dropin.DetectorCoverageWarning):
+        assert dropin.check_detector_coverage(136, 0.5, 96, "SIRT")               # 68 < 136
+    with w.catch_warnings():
+        w.simplefilter("error")
+        assert not dropin.check_detector_coverage(68, 1.0, 48, "backprojection")  # the default row
+        assert not dropin.check_detector_coverage(100, 1.0, 48, "backprojection")
+        assert not dropin.check_detector_coverage(10, 0.0, 48, "SIRT")            # invalid: the library rejects it
