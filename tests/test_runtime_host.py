@@ -42,3 +42,36 @@ def test_detector_coverage_warning():
         assert not dropin.check_detector_coverage(68, 1.0, 48, "backprojection")  # the default row
         assert not dropin.check_detector_coverage(100, 1.0, 48, "backprojection")
         assert not dropin.check_detector_coverage(10, 0.0, 48, "SIRT")            # invalid: the library rejects it
+
+
+class _FakeLib:
+    """Stands in for libsynk: a context whose last call failed with ``rc``."""
+
+    def __init__(self, rc, msg):
+        self.rc, self.msg = rc, msg
+
+    def synk_context_sync(self, handle):
+        return self.rc
+
+    def synk_context_get_error(self, handle):
+        return self.msg.encode()
+
+
+def _fake_context(rc, msg):
+    ctx = object.__new__(rt._Context)
+    ctx.handle, ctx.device, ctx.lib = None, 0, _FakeLib(rc, msg)
+    return ctx
+
+
+def test_timeout_status_reaches_the_caller():
+    """A grid barrier that gave up leaves SYNK_ETIMEOUT in the context; the
+    next sync raises it with the library's message (the failure is made by a
+    fake of the library, no GPU involved)."""
+    from synkrotomo_gb300 import _lib
+    ctx = _fake_context(_lib.SYNK_ETIMEOUT, "persistent SIRT kernel: grid barrier timed out")
+    with pytest.raises(rt.SynkError) as e:
+        ctx.sync()
+    assert e.value.code == _lib.SYNK_ETIMEOUT and "timed out" in str(e.value)
+    with pytest.raises(ValueError):
+        _fake_context(_lib.SYNK_EINVAL, "bad argument").check(_lib.SYNK_EINVAL, "call")
+    _fake_context(0, "").sync()        # status 0: no exception
