@@ -13,8 +13,8 @@ before every step.  e2e: the same metric through the public drop-in API
 host<->device copies inside the timed region.
 
 --impl reference times the reference's CPU path (the FP32 C restatement of
-the Futhark programs, oracle/cpu_ref.c, every host core) on the same
-workload: a bounded sample of angles, scaled to the full angle count.
+the Futhark programs, oracle/cpu_ref.c in its host-tuned build, every host
+core) on the same workload: whole steps, every angle, nothing extrapolated.
 """
 from __future__ import annotations
 
@@ -48,6 +48,15 @@ def set_workload(size, angles, detectors):
 def workload_name():
     return (f"projector microbench, dense on-the-fly: N={N_SIZE} image, {N_ANGLES} angles in [0,pi), "
             f"{N_DET} detectors, deltarho=1")
+
+
+def bench_config(n_gpus):
+    """The workload description both arms print (same dict for the GPU arm and
+    the reference arm)."""
+    return {"workload": workload_name(), "image": N_SIZE, "angles": N_ANGLES, "detectors": N_DET,
+            "step": "forward projection + backprojection",
+            "l2": "flushed (512 MB write) before every step on the GPU; inputs (40.5 MB) exceed no cache on the host",
+            "parallelism": f"replicas x{n_gpus}"}
 
 
 def step_bytes():
@@ -96,37 +105,43 @@ def cpu_model():
 # stand-in for the reference's CPU build)
 # ---------------------------------------------------------------------------
 
-def cpu_reference_rate(budget_s=12.0, seed=0):
-    """Seconds per full FP+BP step of the workload on all host cores,
-    extrapolated from a sample of angles (both projectors are linear in the
-    angle count)."""
+def cpu_reference_step(seed=0):
+    """One whole step of the workload (forward projection of the image and
+    backprojection of the sinogram over all angles) by the CPU port on every
+    host core, timed build: seconds for FP, BP and the step."""
     from oracle import cpu_ref
+    cpu_ref.use_build("timed")
     cores = host_cores()
     cpu_ref.set_threads(cores)
-    g, img, sino = workload(seed)
-    D = N_DET
+    g, img, sino = _cpu_workload(seed)
+    t0 = time.perf_counter()
+    cpu_ref.forwardprojection(g.angles, g.rhozero, g.deltarho, N_DET, img)
+    t1 = time.perf_counter()
+    cpu_ref.backprojection(g.angles, g.rhozero, g.deltarho, N_SIZE, sino)
+    t2 = time.perf_counter()
+    return {"fp_s": t1 - t0, "bp_s": t2 - t1, "step_s": t2 - t0, "cores": cores}
 
-    def run(na):
-        idx = np.linspace(0, N_ANGLES - 1, na).astype(int)
-        ang = g.angles[idx].copy()
-        sub = sino.reshape(N_ANGLES, D)[idx].ravel().copy()
-        t0 = time.perf_counter()
-        cpu_ref.forwardprojection(ang, g.rhozero, g.deltarho, D, img)
-        t1 = time.perf_counter()
-        cpu_ref.backprojection(ang, g.rhozero, g.deltarho, N_SIZE, sub)
-        t2 = time.perf_counter()
-        return t1 - t0, t2 - t1
 
-    na = 4
-    fpt, bpt = run(na)
-    per_angle = (fpt + bpt) / na
-    na2 = int(max(4, min(N_ANGLES, (budget_s * 0.8) / max(per_angle, 1e-6))))
-    if na2 > na:
-        fpt, bpt = run(na2)
-        na = na2
-    scale = N_ANGLES / na
-    return {"fp_s": fpt * scale, "bp_s": bpt * scale, "step_s": (fpt + bpt) * scale, "sample_angles": na,
-            "cores": cores}
+_CPU_WL = {}
+
+
+def _cpu_workload(seed):
+    if seed not in _CPU_WL:
+        _CPU_WL[seed] = workload(seed)
+    return _CPU_WL[seed]
+
+
+def cpu_flags():
+    """The timed CPU build's compiler flags (oracle/Makefile)."""
+    try:
+        r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "flags"], capture_output=True,
+                           text=True, timeout=30)
+        for line in r.stdout.splitlines():
+            if line.strip().startswith("timed:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
 
 
 def cpu_sirt_cfg0(iterations=200):
@@ -136,6 +151,7 @@ def cpu_sirt_cfg0(iterations=200):
     from oracle import cpu_ref
 
     from synkrotomo_gb300 import phantom
+    cpu_ref.use_build("timed")
     cores = host_cores()
     cpu_ref.set_threads(cores)
     g = phantom.geometry(128, 128)
@@ -224,20 +240,6 @@ def measured_peaks():
             return json.load(f)
     except (OSError, ValueError):
         return {}
-
-
-def ncu_traffic(name):
-    """Per-launch DRAM bytes of a kernel from its committed ncu summary
-    (profiles/<name>.md, line 'traffic_bytes_per_launch: X'), else None."""
-    path = os.path.join(ROOT, "profiles", f"{name}.md")
-    try:
-        with open(path) as f:
-            for line in f:
-                if line.strip().startswith("traffic_bytes_per_launch:"):
-                    return float(line.split(":", 1)[1].strip().split()[0])
-    except (OSError, ValueError):
-        pass
-    return None
 
 
 def run_gpu(args, rank, world):
@@ -600,22 +602,28 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
+        # whole steps: every angle of the forward projection and of the
+        # backprojection, W untimed, then K timed (no sampling, no scaling)
         r = None
-        times = []
+        times, fps, bps = [], [], []
         for _ in range(args.warmup + args.steps):
-            r = cpu_reference_rate(budget_s=8.0)
+            r = cpu_reference_step()
             times.append(r["step_s"])
-        step_s = statistics.median(times[args.warmup:])
+            fps.append(r["fp_s"])
+            bps.append(r["bp_s"])
+        timed = times[args.warmup:]
+        step_s = sum(timed) / len(timed)
         value = step_bytes() / step_s / 1e9
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": workload_name(), "l2": "n/a (host CPU)"},
+                "config": bench_config(args.gpus),
                 "cpu_baseline": {"value": value, "unit": "GB/s", "cores": r["cores"], "kind": "port",
-                                 "sample": f"{r['sample_angles']} of {N_ANGLES} angles per step, scaled x"
-                                           f"{N_ANGLES / r['sample_angles']:.1f} (oracle/cpu_ref.c, "
-                                           f"{cpu_model()})"},
-                "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                                 "sample": f"whole steps: all {N_ANGLES} angles of FP and BP per step, mean of "
+                                           f"{args.steps} after {args.warmup} untimed (oracle/cpu_ref.c, "
+                                           f"{cpu_flags()}, {cpu_model()})"},
+                "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "fp_ms": 1e3 * statistics.mean(fps[args.warmup:]), "bp_ms": 1e3 * statistics.mean(bps[args.warmup:])}
         print(json.dumps(line))
         return 0
 
@@ -645,16 +653,14 @@ def main():
     kname = "bp_tile_kernel" if dom == "bp" else "fp_lane_kernel"
     roofline = {"bound": "fp32", "kernel": kname, "achieved": achieved,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                "traffic": ncu_traffic(f"{kname}_dense{N_SIZE}") if N_SIZE == 2048 else None,
+                "traffic": None,
                 "peak_source": f"nominal FP32: {res['sms']} SMs x 128 FMA/clk x 2 x {sm_max:.0f} MHz "
                                "(MEASURED_PEAKS.json has no FP32 figure)",
                 "fp_tflops": fp_tf, "bp_tflops": bp_tf}
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res["step_ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(), "image": N_SIZE, "angles": N_ANGLES, "detectors": N_DET,
-                       "step": "forward projection + backprojection", "l2": "flushed (512 MB write) before every step",
-                       "parallelism": f"replicas x{world}"},
+            "config": bench_config(world),
             "fp_ms": res["fp_ms"], "bp_ms": res["bp_ms"],
             # per step: setup (geometry_kernel when a > 1024, setup_kernel) + fp_lane_kernel + fp_exact_kernel
             # (FP); setup + row_scale_kernel + bp_tile_kernel (BP)
@@ -688,11 +694,11 @@ def main():
             c0 = cpu_sirt_cfg0()
             line["sirt_cfg0"]["cpu_port_200_iterations_ms"] = c0["s"] * 1e3
             line["sirt_cfg0"]["cpu_port_cores"] = c0["cores"]
-        r = cpu_reference_rate(budget_s=10.0)
+        r = cpu_reference_step()
         cv = step_bytes() / r["step_s"] / 1e9
         line["cpu_baseline"] = {"value": cv, "unit": "GB/s", "cores": r["cores"], "kind": "port",
-                                "sample": f"{r['sample_angles']} of {N_ANGLES} angles, scaled to all angles "
-                                          f"(oracle/cpu_ref.c, {cpu_model()})"}
+                                "sample": f"one whole step (all {N_ANGLES} angles of FP and BP; oracle/cpu_ref.c, "
+                                          f"{cpu_flags()}, {cpu_model()})"}
     print(json.dumps(line))
     return 0
 

@@ -57,6 +57,16 @@ int synk_context_set_stream(synk_context *ctx, void *stream);
 /* Waits for the context's stream; returns SYNK_ETIMEOUT if a persistent
  * kernel gave up at a grid barrier, SYNK_ECUDA on an asynchronous CUDA error. */
 int synk_context_sync(synk_context *ctx);
+/* Time limit of every wait inside the library's persistent kernels (the SIRT
+ * grid barrier, the tensor-core engine's mbarrier waits): default 2 s, range
+ * [1 us, 60 s].  A wait that runs out records SYNK_ETIMEOUT, its kernel
+ * returns, and the next synk_context_sync() reports it and clears it.
+ * missing_blocks > 0 is fault injection for testing that path: the grid
+ * barrier of the next persistent SIRT launches waits for that many blocks
+ * more than were launched, so every barrier runs out after timeout_ns.  Pass
+ * 0 in production.  No reference counterpart: the reference surfaces failures
+ * only as the runtime's error codes (futhark's context error string). */
+int synk_context_set_barrier_limit(synk_context *ctx, uint64_t timeout_ns, int32_t missing_blocks);
 /* Message of the last failure on this context ("" when none).  The pointer
  * stays valid until the next call on the context. */
 const char *synk_context_get_error(synk_context *ctx);
@@ -233,9 +243,12 @@ int synk_sanityCheck(synk_context *ctx, uint8_t *out, const float *sane, const f
  * SYNK_NOALLOC_MAX_ANGLES angles (larger counts return SYNK_EINVAL).  Its
  * scratch is one file-scope device array (about 448 KiB) that every GPU
  * loading the library holds until exit.  The first call on a device looks up
- * that array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * that array's device address (cudaGetSymbolAddress) and keeps it for the
+ * life of the process; make that first call before any stream capture.  A
+ * device reset (cudaDeviceReset) invalidates the kept address: this entry
+ * point does not support a reset of a device it has run on.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 #define SYNK_NOALLOC_MAX_ANGLES 8192
 int synk_backprojection_noalloc(synk_context *ctx, float *out, const float *angles, int64_t a, float rhozero,
                                 float deltarho, int32_t size, const float *projections, int64_t p);

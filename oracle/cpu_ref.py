@@ -12,24 +12,39 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libcpuref.so")
-_lib = None
+_TIMED_PATH = os.path.join(_HERE, "_build", "libcpuref_timed.so")
+_libs = {}
+_active = "parity"
 
 _f32p = ctypes.POINTER(ctypes.c_float)
 
 
 def build(force: bool = False) -> str:
-    """Compile ``cpu_ref.c`` with the recipe in ``oracle/Makefile``."""
+    """Compile ``cpu_ref.c`` (parity and timed builds) with ``oracle/Makefile``."""
     src = os.path.join(_HERE, "cpu_ref.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    stale = any(not os.path.exists(p) or os.path.getmtime(p) < os.path.getmtime(src) for p in (_LIB_PATH, _TIMED_PATH))
+    if force or stale:
         subprocess.run(["make", "-s", "-C", _HERE, "-B" if force else "all"], check=True)
     return _LIB_PATH
 
 
+def use_build(kind: str) -> str:
+    """Select the library the functions below call: "parity" (the default:
+    float32 rounding as written, what the tests compare with) or "timed" (the
+    same source tuned for the host CPU, what bench.py times).  Returns the
+    previous selection."""
+    global _active
+    if kind not in ("parity", "timed"):
+        raise ValueError(f"unknown cpu_ref build {kind!r}")
+    prev, _active = _active, kind
+    return prev
+
+
 def lib():
-    global _lib
-    if _lib is None:
+    L = _libs.get(_active)
+    if L is None:
         build()
-        L = ctypes.CDLL(_LIB_PATH)
+        L = ctypes.CDLL(_LIB_PATH if _active == "parity" else _TIMED_PATH)
         L.cpuref_forwardprojection.argtypes = [_f32p, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int,
                                                _f32p, ctypes.c_int64, _f32p]
         L.cpuref_backprojection.argtypes = [_f32p, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int,
@@ -40,8 +55,8 @@ def lib():
                                     ctypes.c_int, _f32p]
         L.cpuref_last_oob.restype = ctypes.c_int64
         L.cpuref_set_threads.argtypes = [ctypes.c_int]
-        _lib = L
-    return _lib
+        _libs[_active] = L
+    return L
 
 
 def _p(a):

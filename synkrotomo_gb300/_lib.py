@@ -65,6 +65,7 @@ SIGNATURES = {
     "synk_context_free": (None, [c_ctx]),
     "synk_context_set_stream": (ctypes.c_int, [c_ctx, ctypes.c_void_p]),
     "synk_context_sync": (ctypes.c_int, [c_ctx]),
+    "synk_context_set_barrier_limit": (ctypes.c_int, [c_ctx, ctypes.c_uint64, ctypes.c_int32]),
     "synk_context_get_error": (ctypes.c_char_p, [c_ctx]),
     "synk_version": (ctypes.c_char_p, []),
     "synk_forwardprojection": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_float,

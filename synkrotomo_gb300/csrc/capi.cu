@@ -35,6 +35,7 @@ struct synk_context {
     std::string err;
     int *d_status = nullptr;   // written by persistent kernels (SYNK_ETIMEOUT)
     unsigned long long barrier_timeout_ns = 2000000000ull;
+    unsigned barrier_extra = 0;   // fault injection: blocks a grid barrier waits for that never come
 };
 
 namespace {
@@ -414,6 +415,7 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
     sp.work = words + 4;
     sp.status = ctx->d_status;
     sp.timeout_ns = ctx->barrier_timeout_ns;
+    sp.barrier_extra = ctx->barrier_extra;
     sp.tol2 = tol > 0.0 ? tol * tol : 0.0;
     sp.record_final = want_res ? 1 : 0;
     sp.dynamic = nprob > 1 ? 1 : 0;
@@ -542,6 +544,19 @@ int synk_context_sync(synk_context *ctx) {
             return fail(ctx, SYNK_ETIMEOUT, "a grid barrier of the persistent SIRT kernel timed out; the result is invalid");
         return fail(ctx, status, "device status %d", status);
     }
+    return SYNK_OK;
+}
+
+int synk_context_set_barrier_limit(synk_context *ctx, uint64_t timeout_ns, int32_t missing_blocks) {
+    if (!ctx) return SYNK_EINVAL;
+    ctx->err.clear();
+    if (timeout_ns < 1000ull || timeout_ns > 60000000000ull)
+        return fail(ctx, SYNK_EINVAL, "barrier time limit must be in [1 us, 60 s] (got %llu ns)",
+                    (unsigned long long)timeout_ns);
+    if (missing_blocks < 0 || missing_blocks > 1024)
+        return fail(ctx, SYNK_EINVAL, "missing_blocks must be in [0, 1024] (got %d)", missing_blocks);
+    ctx->barrier_timeout_ns = timeout_ns;
+    ctx->barrier_extra = (unsigned)missing_blocks;
     return SYNK_OK;
 }
 

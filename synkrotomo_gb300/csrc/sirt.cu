@@ -297,7 +297,7 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
 
 __global__ void __launch_bounds__(256, 3) sirt_persistent_kernel(SirtParams p) {
     __shared__ SirtShared sh;
-    const unsigned nb = gridDim.x;
+    const unsigned nb = gridDim.x + p.barrier_extra;
     for (int it = 0; it <= p.max_iterations; ++it) {
         // phase 2*it: FP.  Rotating counters: reset the one of the phase after next.
         const int ph = 2 * it;

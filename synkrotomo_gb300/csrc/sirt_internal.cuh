@@ -42,6 +42,7 @@ struct SirtParams {
     unsigned *work;       // [3] rotating work counters (dynamic assignment)
     int *status;          // SYNK_OK or SYNK_ETIMEOUT
     unsigned long long timeout_ns;
+    unsigned barrier_extra;   // blocks the grid barrier waits for beyond the grid (fault injection; 0)
     double tol2;          // relative tolerance squared (0: no stopping rule)
     int record_final;     // also measure the residual of each problem's final iterate
     int dynamic;          // hand out items with an atomic counter (uneven batches)

@@ -57,6 +57,13 @@ class _Context:
         rc = self.lib.synk_context_sync(self.handle)
         self.check(rc, "synk_context_sync")
 
+    def set_barrier_limit(self, timeout_ns: int = 2_000_000_000, missing_blocks: int = 0):
+        """Time limit of the persistent kernels' waits; ``missing_blocks`` > 0
+        injects a barrier that waits for blocks that never arrive (testing
+        the SYNK_ETIMEOUT path; 0 in production)."""
+        self.check(self.lib.synk_context_set_barrier_limit(self.handle, int(timeout_ns), int(missing_blocks)),
+                   "synk_context_set_barrier_limit")
+
 
 _contexts: dict[int, _Context] = {}
 _ctx_lock = threading.Lock()

@@ -117,20 +117,34 @@ def gather_items(local: Dict[int, torch.Tensor], owner: Sequence[int], group=Non
     world, rank = world_rank(group)
     n = len(owner)
     mine = {i for i in range(n) if owner[i] == rank}
-    if set(local) != mine:
-        raise ValueError(f"rank {rank} holds items {sorted(local)} but owns {sorted(mine)}")
-    for i, t in local.items():
-        if t.dtype != dtype:
-            raise TypeError(f"item {i} is {t.dtype}, expected {dtype}")
+    wrong_items = set(local) != mine
+    wrong_dtype = [i for i, t in local.items() if t.dtype != dtype]
+
+    def raise_local():
+        if wrong_items:
+            raise ValueError(f"rank {rank} holds items {sorted(local)} but owns {sorted(mine)}")
+        if wrong_dtype:
+            i = wrong_dtype[0]
+            raise TypeError(f"item {i} is {local[i].dtype}, expected {dtype}")
+
     if world == 1:
+        raise_local()
         return [local[i].reshape(-1) for i in range(n)]
     d = _dist()
     dev = _comm_device(group)
-    # every rank must hold the same assignment (it is computed, not exchanged):
-    # compare a checksum with one min/max reduction, and raise on every rank alike
+    # Every rank must hold the same assignment (it is computed, not exchanged)
+    # and its own items in the right dtype.  One MAX reduction carries a
+    # checksum of the assignment (as +sig and -sig) and the ranks' local
+    # failures, so that all ranks raise together instead of one rank raising
+    # while the others wait in the next collective.
     sig = float(zlib.crc32(np.asarray(owner, dtype=np.int64).tobytes())) + 2.0 ** 32 * n
-    chk = torch.tensor([sig, -sig], dtype=torch.float64, device=dev)
+    chk = torch.tensor([sig, -sig, float(wrong_items), float(bool(wrong_dtype))], dtype=torch.float64, device=dev)
     d.all_reduce(chk, op=d.ReduceOp.MAX, group=group)
+    if wrong_items or wrong_dtype:
+        raise_local()
+    if chk[2].item() or chk[3].item():
+        kind = ValueError if chk[2].item() else TypeError
+        raise kind("another rank holds a wrong item set or dtype for the gather")
     if chk[0].item() != -chk[1].item():
         raise ValueError("the ranks hold different item assignments (different costs or item counts)")
     lens = torch.zeros(max(n, 1), dtype=torch.int64, device=dev)

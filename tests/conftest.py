@@ -33,3 +33,19 @@ def rel_l2(a, b):
     b = np.asarray(b, np.float64)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (nb if nb else 1.0))
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_fpinput512():
+    """The reference's dataset futhark/data/fpinputf32rad512 (the five arguments
+    of forwardprojection.main) from its exact copy tests/golden/fpinputf32rad512.npz.
+    A missing fixture is an error, not a skip."""
+    path = os.path.join(GOLDEN, "fpinputf32rad512.npz")
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing (write it with tests/golden/make_fpinput512.py)")
+    z = np.load(path)
+    image = z["levels"][z["codes"]].astype(np.float32)
+    return (z["angles"].astype(np.float32), np.float32(z["rhozero"]), np.float32(z["deltarho"]),
+            np.int32(z["numrhos"]), image)

@@ -33,6 +33,11 @@ def test_reference_arm_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+    # whole steps, nothing scaled; the same config dict as the GPU arm prints
+    assert "whole steps" in cb["sample"] and "scaled" not in cb["sample"]
+    b = _bench_module()
+    b.set_workload(64, 16, 0)
+    assert d["config"] == b.bench_config(d["n_gpus"])
 
 
 def test_reference_arm_other_ranks_print_nothing():

@@ -1,5 +1,6 @@
 """Futhark value files (text and binary) and the futhark-bench-style harness
 logic: CPU only."""
+import hashlib
 import io
 import os
 
@@ -7,8 +8,11 @@ import numpy as np
 import pytest
 
 from synkrotomo_gb300 import fbench, fvalues
+from tests.conftest import GOLDEN, load_fpinput512
 
-REF_DATASET = "/root/reference/futhark/data/fpinputf32rad512"
+# directory holding the reference's own dataset files (optional: the exact
+# copy under tests/golden/ is what the tests run on)
+REF_DATA_DIR = os.environ.get("SYNK_REFERENCE_DATA", "")
 
 
 def test_text_scalars_and_suffixes():
@@ -99,10 +103,7 @@ def test_dataset_size_and_csv(tmp_path):
     assert p.read_text() == "64;225.40\n128;348.10\n"
 
 
-@pytest.mark.skipif(not os.path.exists(REF_DATASET), reason="the reference's dataset is not on this machine")
-def test_reads_the_reference_dataset():
-    """data/fpinputf32rad512: forwardprojection.main's five arguments."""
-    vals = fvalues.read_file(REF_DATASET)
+def _check_fpinput512(vals):
     args = fbench.parse_args_for("forwardprojection", vals)
     angles, rz, dr, nr, img = args
     assert angles.shape == (805,) and angles.dtype == np.float32
@@ -111,3 +112,27 @@ def test_reads_the_reference_dataset():
     assert img.shape == (512 * 512,) and np.count_nonzero(img) == 205859
     back = fvalues.read_values(fvalues.write_binary(vals))
     assert all(_same(a, b) for a, b in zip(vals, back))
+    return args
+
+
+def test_reference_dataset_copy_round_trips():
+    """The exact copy of data/fpinputf32rad512 (forwardprojection.main's five
+    arguments) written in both value formats and read back."""
+    angles, rz, dr, nr, img = load_fpinput512()
+    vals = [angles, rz, dr, nr, img]
+    _check_fpinput512(vals)
+    text = fvalues.write_text(vals)
+    assert all(_same(a, b) for a, b in zip(vals, fvalues.read_values(text)))
+
+
+@pytest.mark.skipif(not REF_DATA_DIR, reason="SYNK_REFERENCE_DATA (the reference's futhark/data directory) not set")
+def test_reads_the_reference_dataset():
+    """data/fpinputf32rad512 itself, when its directory is given: it parses to
+    the values of the committed copy."""
+    path = os.path.join(REF_DATA_DIR, "fpinputf32rad512")
+    raw = open(path, "rb").read()
+    args = _check_fpinput512(fvalues.read_values(raw))
+    copy = load_fpinput512()
+    assert all(_same(a, b) for a, b in zip(args, copy))
+    z = np.load(os.path.join(GOLDEN, "fpinputf32rad512.npz"))
+    assert str(z["source_sha256"]) == hashlib.sha256(raw).hexdigest()

@@ -198,3 +198,47 @@ def test_ranks_with_different_assignments_fail_together():
             if p.is_alive():
                 p.kill()
     assert got == {0: "ValueError", 1: "ValueError"}
+
+
+def _local_fault_worker(rank, world, port, q, fault):
+    import torch.distributed as dist
+    try:
+        dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+        owner = [0, 1, 0, 1]
+        local = {i: torch.zeros(3) for i in range(4) if owner[i] == rank}
+        if rank == 1 and fault == "items":
+            local[2] = torch.zeros(3)               # an item rank 0 owns
+        if rank == 1 and fault == "dtype":
+            local[1] = torch.zeros(3, dtype=torch.float64)
+        try:
+            shard.gather_items(local, owner)
+            q.put((rank, "no error"))
+        except (ValueError, TypeError) as e:
+            q.put((rank, type(e).__name__))
+        dist.destroy_process_group()
+    except Exception as e:
+        q.put((rank, repr(e)))
+
+
+@pytest.mark.parametrize("fault,kind", [("items", "ValueError"), ("dtype", "TypeError")])
+def test_a_local_fault_on_one_rank_fails_every_rank(fault, kind):
+    """One rank passes a wrong item set or dtype: both ranks raise (none is
+    left waiting in a collective)."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_local_fault_worker, args=(k, world, port, q, fault)) for k in range(world)]
+    for p in procs:
+        p.start()
+    got = {}
+    try:
+        for _ in range(world):
+            rank, what = q.get(timeout=240)
+            got[rank] = what
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.is_alive():
+                p.kill()
+    assert got == {0: kind, 1: kind}
