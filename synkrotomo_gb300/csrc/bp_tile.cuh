@@ -6,8 +6,9 @@
 // the chord-length trapezoid are staged in shared memory 64 angles at a time
 // and read as one broadcast float4 + one float2 per angle; each (pixel, angle)
 // then costs ~14 FP32/INT instructions and two sinogram gathers:
-//   q    = x_c*cos - y_c*sin - rhozero            (rho of the centre, shifted)
-//   s0   = ceil((q - sqrt(2)/2) / deltarho)       (first candidate detector)
+//   q    = x_c*cos - y_c*sin - rz_c               (rho of the centre from the middle
+//                                                  detector position rz_c, ProbGeom)
+//   s0   = ceil((q - sqrt(2)/2) / deltarho) + zi  (first candidate detector)
 //   d_i  = s0*deltarho + i*deltarho - q           (signed distance ray -> centre)
 //   w_i  = sat((h - |d_i|) / b)                   (chord / lbase)
 //   acc += lbase * sum_i w_i * sino[k][s0 + i]
@@ -50,8 +51,8 @@ __device__ __forceinline__ void bp_stage(const ProbGeom &P, int k0, BpStage &st)
 // staged chunk into acc[m] for the PIX pixels (row0 + m*ystep, col) whose
 // centres are (xc, yc0 + m*ystep).  sino: the problem's sinogram [a][D].
 //
-// UNIT (deltarho = 1): with q = rho_c - rhozero - sqrt(2)/2, the first
-// candidate detector is s0 = ceil(q) and e = s0 - q is in [0, 1); the two
+// UNIT (deltarho = 1): with q = rho_c - rz_c - sqrt(2)/2, the first
+// candidate detector is ceil(q) + zi and e = ceil(q) - q is in [0, 1); the two
 // candidates sit at signed distances e - sqrt(2)/2 and e + 1 - sqrt(2)/2
 // from the centre (the second is never negative), so
 //   w0 = sat(h/b - |e - sqrt(2)/2| / b),  w1 = sat(c1 - e/b),  c1 = h/b - (1 - sqrt(2)/2)/b.
@@ -67,7 +68,9 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
     const int D = P.D;
     const unsigned uD = (unsigned)D;
     const int nk = min(kBpChunk, kend - kc);
-    const float zoff = -P.rhozero - fact;
+    const float zoff = -P.rz_c - fact;        // centred: |q| stays below ~N/sqrt(2) + 1
+    // INRANGE gather base: row + zi - kMagicBits (the magic constant's bits folded in)
+    const uintptr_t zoffb = (uintptr_t)(((intptr_t)P.zi - (intptr_t)kMagicBits) * 4);
     for (int i = kphase; i < nk; i += kstride) {
         const float4 g = st.cs[i];
         const float2 le = st.le[i];
@@ -82,7 +85,7 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
             // INRANGE: the address comes straight from the bits of the rounded
             // sum r = q + 1.5*2^23 (bits(r) = bits(1.5*2^23) + s0), that constant
             // folded into the row base: one wide multiply-add per gather pair
-            const uintptr_t rowb = reinterpret_cast<uintptr_t>(row) - (uintptr_t)kMagicBits * 4u;
+            const uintptr_t rowb = reinterpret_cast<uintptr_t>(row) + zoffb;
 #pragma unroll
             for (int m = 0; m < PIX; ++m) {
                 const float q = m ? fmaf((float)m, dq, q0) : q0;
@@ -97,6 +100,7 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
                 } else {
                     int s0;
                     e = ceil_magic(q, s0) - q;
+                    s0 += P.zi;
                     v0 = ((unsigned)s0 < uD) ? __ldg(row + s0) : 0.0f;
                     v1 = ((unsigned)(s0 + 1) < uD) ? __ldg(row + s0 + 1) : 0.0f;
                 }
@@ -106,18 +110,18 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
                 else acc[m] = fmaf(le.x, fmaf(w1, v1, w0 * v0), acc[m]);
             }
         } else {
-            const float t0 = fmaf(-yc0, g.y, -P.rhozero);
+            const float t0 = fmaf(-yc0, g.y, -P.rz_c);
             const float tstep = -ystep * g.y;
 #pragma unroll
             for (int m = 0; m < PIX; ++m) {
                 const float t = m ? fmaf((float)m, tstep, t0) : t0;
-                const float qc = fmaf(xc, g.x, t);             // rho_c - rhozero
+                const float qc = fmaf(xc, g.x, t);             // rho_c - rz_c
                 int s0;
                 float s0f = ceil_magic((qc - fact) * P.inv_deltarho, s0);
                 float d = s0f * P.deltarho - qc;
                 float a = 0.0f;
                 for (int q2 = 0; q2 < P.rpp; ++q2, d += P.deltarho) {
-                    const int det = s0 + q2;
+                    const int det = s0 + P.zi + q2;
                     const float w = __saturatef(fmaf(-fabsf(d), g.w, g.z));
                     if ((unsigned)det < uD) a = fmaf(w, __ldg(row + det), a);
                 }

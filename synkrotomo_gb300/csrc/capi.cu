@@ -160,6 +160,11 @@ ProbGeom make_geom(int64_t a, float rhozero, float deltarho, int64_t numrhos, in
     P.rhozero = rhozero;
     P.deltarho = deltarho;
     P.inv_deltarho = 1.0f / deltarho;
+    // the detector nearest rho = 0: zi = round(-rhozero/deltarho), rz_c its
+    // position (exact in f32 for deltarho = 1: rhozero + an integer)
+    const double zi = nearbyint(-(double)rhozero / (double)deltarho);
+    P.zi = (int)zi;
+    P.rz_c = (float)((double)rhozero + zi * (double)deltarho);
     P.geom = geom;
     return P;
 }
@@ -333,10 +338,19 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         const size_t n = (size_t)q.size * q.size, pr = (size_t)q.a * q.numrhos;
         const size_t np = (size_t)q.size * (q.size + 2), K = (size_t)q.iterations + 1;
         AngleGeom *geom;
-        float *R, *C, *xpad, *xTpad, *rr;
+        float *R, *C, *xpad, *xTpad, *rr, *glen, *gcontrib;
         double *res2, *b2;
-        int *stop_iter;
+        int *stop_iter, *goff;
+        int2 *graze;
+        // rays that only clip a corner pixel: per corner and angle at most
+        // ceil(1/deltarho) + 1 (graze_list_kernel)
+        const double gcapc = (double)q.a * (ceil(1.0 / (double)q.deltarho) + 1.0);
+        const int graze_capc = (int)std::max(1.0, std::min({gcapc, (double)pr, (double)(1 << 26)}));
         SYNK_CUDA(sc.get(&geom, (size_t)q.a), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&graze, 4 * (size_t)graze_capc), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&glen, 4 * (size_t)graze_capc), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&gcontrib, 4 * (size_t)graze_capc * q.nslices), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&goff, 5), "cudaMallocAsync");
         SYNK_CUDA(sc.get(&R, pr), "cudaMallocAsync(R)");
         SYNK_CUDA(sc.get(&C, n), "cudaMallocAsync(C)");
         SYNK_CUDA(sc.get(&xpad, np * q.nslices), "cudaMallocAsync(padded image)");
@@ -351,10 +365,17 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         SYNK_CUDA(cudaGetLastError(), "fill kernel");
         h.P = make_geom(q.a, q.rhozero, q.deltarho, q.numrhos, q.size, geom);
         SYNK_CUDA(make_setup(sc, q.angles, h.P, &h.L, st), "setup kernel");
-        SYNK_CUDA(launch_normalisers(h.P, R, C, st), "normaliser kernels");
+        SYNK_CUDA(launch_normalisers(h.P, R, C, graze, glen, goff, graze_capc, st), "normaliser kernels");
+        // the listed rays' entries stay zero (their terms go to the corner pixels)
+        SYNK_CUDA(cudaMemsetAsync(rr, 0, sizeof(float) * pr * q.nslices, st), "memset");
         SYNK_CUDA(launch_pad(q.out, xpad, xTpad, q.size, q.nslices, st), "pad kernel");
         SYNK_CUDA(launch_sumsq(q.projections, pr, q.nslices, b2, st), "norm kernel");
         h.R = R;
+        h.graze = graze;
+        h.glen = glen;
+        h.gcontrib = gcontrib;
+        h.goff = goff;
+        h.graze_capc = graze_capc;
         h.C = C;
         h.b = q.projections;
         h.xpad = xpad;

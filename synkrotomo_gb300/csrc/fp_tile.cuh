@@ -12,8 +12,8 @@
 //   fp_lane_ray (SIRT, whose iterate is kept padded): row stride N+2, a zero
 //     column on each side, so one predicate covers both 4-byte gathers.
 // Per lane and row (forwardprojection.fut:31-56):
-//   u  = j*slope + u0                  left end of the row segment, pixel units
-//   c  = floor(u), t = max(0, (u - c + |slope| - 1) / |slope|)   share of c+1
+//   x  = (j - half)*slope + x0         left end of the row segment, centred
+//   c  = floor(x) + half, t = max(0, (x - floor(x) + |slope| - 1) / |slope|)   share of c+1
 //   s += v[c] + t*(v[c+1] - v[c])      (times lbase once per ray)
 // Near-axis angles are listed separately and run the reference's own
 // expressions (fp_exact in project.cu / the SIRT kernel).
@@ -33,21 +33,34 @@ struct AngleLists {
     const int *counts;   // device: steep groups, flat groups, near-axis angles
 };
 
-// Row range [j0, j1) in which the ray's segment can touch a column of [0, N).
-__device__ __forceinline__ void lane_rows(const ProbGeom &P, const AngleGeom &g, float u0, int &j0, int &j1) {
-    j0 = 0;
-    j1 = P.N;
-    const float aslope = fabsf(g.slope);
-    if (g.slope != 0.0f) {
-        const float ja = (-1.0f - aslope - u0) / g.slope;
-        const float jb = ((float)P.N - u0) / g.slope;
-        const float lo = fmaxf(fminf(ja, jb) - 1.0f, 0.0f);
-        const float hi = fminf(fmaxf(ja, jb) + 2.0f, (float)P.N);
-        j0 = (int)lo;
-        j1 = (hi > lo) ? (int)hi : j0;
-    } else if (!(u0 > -1.0f && u0 < (float)P.N)) {
-        j1 = j0;
-    }
+// Row range [j0, j1) in which the ray's segment can touch a column of [0, N)
+// (x0: ray_x0).
+__device__ __forceinline__ void lane_rows(const ProbGeom &P, const AngleGeom &g, float x0, int &j0, int &j1) {
+    ray_rows(P, g, x0, j0, j1);
+}
+
+// Ray sum of detector r for angle geometry g by one thread with the
+// reference's own expressions (forwardprojection.fut:31-56), rows in the
+// reference's order and float32 accumulation, so the value is the f32
+// reference's bit for bit.  img_frame points at pixel (0, 0) of the frame
+// image (the transposed image for flat lines), rows `stride` floats apart;
+// ONES reads no image.  Rows whose segment cannot touch the image add exactly
+// zero in the reference and are skipped (the fast path's row clip with its
+// margins).  Used for the chords of rays that clip one corner pixel, which the
+// two float32 formulations round differently enough to matter once SIRT
+// divides by them.
+template <bool ONES>
+__device__ __forceinline__ float fp_ray_exact_f32(const ProbGeom &P, const AngleGeom &g,
+                                                  const float *__restrict__ img_frame, int stride, int r) {
+    const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));    // forwardprojection.fut:28
+    if (fabsf(rho) > 0.75f * (float)P.N + 2.0f) return 0.0f;
+    const float intercept = __fdiv_rn(rho, g.cost);                               // forwardprojection.fut:29
+    int j0 = 0, j1 = P.N;
+    if (!g.exact) lane_rows(P, g, ray_x0(g, intercept), j0, j1);
+    float acc = 0.0f;
+    for (int j = j0; j < j1; ++j)
+        acc = __fadd_rn(acc, fp_row_exact<ONES>(img_frame, stride, P.half, g.slope, intercept, g.lbase, j - P.half));
+    return acc;
 }
 
 // Sum over frame rows [jb, je) of detector r for the lane's angle k (k < 0:
@@ -58,9 +71,9 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
     const AngleGeom g = load_geom(P.geom, k >= 0 ? k : 0);
     const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));    // forwardprojection.fut:28
     const float intercept = __fdiv_rn(rho, g.cost);                               // forwardprojection.fut:29
-    const float u0 = ray_u0(P, g, intercept);
+    const float x0 = ray_x0(g, intercept);
     int j0 = 0, j1 = 0;
-    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, u0, j0, j1);
+    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, x0, j0, j1);
     j0 = max(j0, jb);
     j1 = min(j1, je);
     if (j1 <= j0) { j0 = je; j1 = je; }
@@ -69,15 +82,17 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
     const float slope = g.slope, ainv = g.ainv;
     const int stride = P.N + 2;
     const unsigned lim = (unsigned)P.N;     // c + 1 in [0, N]
-    // u of rows j..j+3 from one float row counter: u0 + k*slope per lane
-    const float u1 = u0 + slope, u2 = u0 + 2.0f * slope, u3 = u0 + 3.0f * slope;
+    const int half = P.half;
+    const float *img_c = img_pad + half + 1;   // centred column 0 of frame row 0
+    // x of rows j..j+3 from one float row counter: x0 + k*slope per lane
+    const float x1 = x0 + slope, x2 = x0 + 2.0f * slope, x3 = x0 + 3.0f * slope;
     float sum = 0.0f, comp = 0.0f;
-    auto row = [&](float u, int jrow, float &part) {
-        int c;
-        const float fl = floor_magic(u, c);
-        const float t = right_share(u, fl, ainv);
-        const bool ok = (unsigned)(c + 1) <= lim;
-        const float *p = img_pad + (jrow * stride + c + 1);
+    auto row = [&](float x, int jrow, float &part) {
+        int c;                                  // centred column
+        const float fl = floor_magic(x, c);
+        const float t = right_share(x, fl, ainv);
+        const bool ok = (unsigned)(c + half + 1) <= lim;
+        const float *p = img_c + (jrow * stride + c);
         const float v0 = ok ? __ldg(p) : 0.0f;
         const float v1 = ok ? __ldg(p + 1) : 0.0f;
         part += fmaf(t, v1 - v0, v0);
@@ -85,14 +100,14 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
     for (int j = J0; j < J1;) {
         const int jend = min(j + 32, J1);
         float part = 0.0f;
-        float jf = (float)j;
+        float jf = (float)(j - half);
         for (; j + 3 < jend; j += 4, jf += 4.0f) {
-            row(fmaf(jf, slope, u0), j, part);
-            row(fmaf(jf, slope, u1), j + 1, part);
-            row(fmaf(jf, slope, u2), j + 2, part);
-            row(fmaf(jf, slope, u3), j + 3, part);
+            row(fmaf(jf, slope, x0), j, part);
+            row(fmaf(jf, slope, x1), j + 1, part);
+            row(fmaf(jf, slope, x2), j + 2, part);
+            row(fmaf(jf, slope, x3), j + 3, part);
         }
-        for (; j < jend; ++j, jf += 1.0f) row(fmaf(jf, slope, u0), j, part);
+        for (; j < jend; ++j, jf += 1.0f) row(fmaf(jf, slope, x0), j, part);
         comp_add(sum, comp, part);
     }
     return k >= 0 ? (sum + comp) * g.lbase : 0.0f;
@@ -102,8 +117,8 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
 // pad(j, i)) for i in [0, N+1], where pad(j, i) = pixel (j, i-1) and 0 outside
 // [1, N]; entry N+1 of every row is (0, 0).  One 8-byte gather per row serves
 // both pixels of the row segment (v0 + t*(v1 - v0) is one FMA on the entry).
-// Its index comes from the bits of r = u + kMagic rounded down,
-// c + 1 = bits(r) - (kMagicBits - 1), clamped as unsigned to N+1: a segment
+// Its index comes from the bits of r = x + kMagic rounded down,
+// c + 1 = bits(r) - (kMagicBits - 1 - half), clamped as unsigned to N+1: a segment
 // left of column -1 wraps to a huge value and one right of N-1 exceeds N, and
 // both read the zero entry.  The loads are unconditional, so the rows of one
 // unrolled step issue their gathers back to back.
@@ -112,9 +127,9 @@ __device__ __forceinline__ float fp_lane_ray_pair(const ProbGeom &P, int k, int 
     const AngleGeom g = load_geom(P.geom, k >= 0 ? k : 0);
     const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));    // forwardprojection.fut:28
     const float intercept = __fdiv_rn(rho, g.cost);                               // forwardprojection.fut:29
-    const float u0 = ray_u0(P, g, intercept);
+    const float x0 = ray_x0(g, intercept);
     int j0 = 0, j1 = 0;
-    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, u0, j0, j1);
+    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, x0, j0, j1);
     j0 = max(j0, jb);
     j1 = min(j1, je);
     if (j1 <= j0) { j0 = je; j1 = je; }
@@ -123,14 +138,15 @@ __device__ __forceinline__ float fp_lane_ray_pair(const ProbGeom &P, int k, int 
     const float slope = g.slope, ainv = g.ainv;
     const uintptr_t rowbytes = (uintptr_t)(P.N + 2) * 8u;
     const unsigned zix = (unsigned)P.N + 1u;                   // the zero entry of a row
-    const unsigned okbase = (unsigned)kMagicBits - 1u;         // bits(r) - okbase = c + 1
+    // bits(r) - okbase = c + 1 with c = floor(x) + half the pixel index
+    const unsigned okbase = (unsigned)kMagicBits - 1u - (unsigned)P.half;
     const uintptr_t base = reinterpret_cast<uintptr_t>(pair);
-    const float u1 = u0 + slope, u2 = u0 + 2.0f * slope, u3 = u0 + 3.0f * slope;
+    const float x1 = x0 + slope, x2 = x0 + 2.0f * slope, x3 = x0 + 3.0f * slope;
     float sum = 0.0f, comp = 0.0f;
-    auto row = [&](float u, uintptr_t rowb, float &part) {
-        const float rr = __fadd_rd(u, kMagic);
+    auto row = [&](float x, uintptr_t rowb, float &part) {
+        const float rr = __fadd_rd(x, kMagic);
         const float fl = __fsub_rn(rr, kMagic);
-        const float t = right_share(u, fl, ainv);
+        const float t = right_share(x, fl, ainv);
         const unsigned ix = min((unsigned)__float_as_int(rr) - okbase, zix);
         const float2 v = __ldg(reinterpret_cast<const float2 *>(rowb + (uintptr_t)ix * 8u));
         part += fmaf(t, v.y, v.x);
@@ -138,15 +154,15 @@ __device__ __forceinline__ float fp_lane_ray_pair(const ProbGeom &P, int k, int 
     for (int j = J0; j < J1;) {
         const int jend = min(j + 32, J1);
         float part = 0.0f;
-        float jf = (float)j;
+        float jf = (float)(j - P.half);
         uintptr_t rowb = base + (uintptr_t)j * rowbytes;
         for (; j + 3 < jend; j += 4, jf += 4.0f, rowb += 4 * rowbytes) {
-            row(fmaf(jf, slope, u0), rowb, part);
-            row(fmaf(jf, slope, u1), rowb + rowbytes, part);
-            row(fmaf(jf, slope, u2), rowb + 2 * rowbytes, part);
-            row(fmaf(jf, slope, u3), rowb + 3 * rowbytes, part);
+            row(fmaf(jf, slope, x0), rowb, part);
+            row(fmaf(jf, slope, x1), rowb + rowbytes, part);
+            row(fmaf(jf, slope, x2), rowb + 2 * rowbytes, part);
+            row(fmaf(jf, slope, x3), rowb + 3 * rowbytes, part);
         }
-        for (; j < jend; ++j, jf += 1.0f, rowb += rowbytes) row(fmaf(jf, slope, u0), rowb, part);
+        for (; j < jend; ++j, jf += 1.0f, rowb += rowbytes) row(fmaf(jf, slope, x0), rowb, part);
         comp_add(sum, comp, part);
     }
     return k >= 0 ? (sum + comp) * g.lbase : 0.0f;

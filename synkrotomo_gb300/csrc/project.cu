@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) fp_lane_kernel(ProbGeom P, AngleLists L, 
 // of dependent gathers is short.  The per-ray arithmetic is fp_lane_kernel's
 // (fp_lane_ray_pair); the S partial sums are added in a fixed order.
 template <int S>
-__global__ void __launch_bounds__(1024) fp_det_kernel(ProbGeom P, AngleLists L, const float2 *__restrict__ xpair,
+__global__ void __launch_bounds__(1024, 2) fp_det_kernel(ProbGeom P, AngleLists L, const float2 *__restrict__ xpair,
                                                       const float2 *__restrict__ xTpair, float *__restrict__ sino) {
     __shared__ float red[32][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -628,6 +628,8 @@ cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino,
 // ---- normalisers (FP64 sums) -----------------------------------------------------------
 
 // R = safe_inverse(A*1): one thread per ray (SIRT.fut:22-23, sirtlib.fut:9-13).
+// R is stored negated for the rays that only clip a corner pixel (see below);
+// graze_list_kernel lists them and the SIRT phases read the sign.
 __global__ void __launch_bounds__(256) rownorm_kernel(ProbGeom P, float *__restrict__ R) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k = blockIdx.y * 8 + warp;
@@ -635,7 +637,98 @@ __global__ void __launch_bounds__(256) rownorm_kernel(ProbGeom P, float *__restr
     if (k >= P.a || r >= P.D) return;
     const AngleGeom g = load_geom(P.geom, k);
     const double v = fp_ray<true>(P, g, nullptr, r, 0, P.N);
-    R[(size_t)k * P.D + r] = v != 0.0 ? (float)(1.0 / v) : 0.0f;
+    float Rv = v != 0.0 ? (float)(1.0 / v) : 0.0f;
+    if (v > 0.0 && v < 1.0 && !g.exact) {
+        // A chord under 1 cuts off a corner of the image inside one corner
+        // pixel.  There R = 1/chord magnifies the chord's rounding (the fast
+        // row rule and the backprojector's trapezoid differ by up to a few
+        // per cent on such rays), so the chord is the reference's own f32 sum
+        // (sirtlib.fut:9-13 inverse of forwardprojection.fut:31-56), which
+        // equals the reference's backprojection weight for that pixel bit for
+        // bit.  The sign sends the ray to the SIRT kernels' exact treatment
+        // (sirt.cu); near-axis angles already take the exact path.
+        const float e = fp_ray_exact_f32<true>(P, g, nullptr, 0, r);
+        if (e != 0.0f) Rv = -__fdiv_rn(1.0f, e);
+    }
+    R[(size_t)k * P.D + r] = Rv;
+}
+
+// The corner pixel a listed ray clips: the corner of the image square with
+// the extreme rho = x cos - y sin on the ray's side (x = +-half at columns
+// N-1 / 0, y = +-half at rows N-1 / 0); 0: row 0 col 0, 1: row 0 col N-1,
+// 2: row N-1 col 0, 3: row N-1 col N-1.
+__device__ __forceinline__ int graze_corner(const AngleGeom &g, float rho) {
+    const bool right = (rho > 0.0f) == (g.c > 0.0f);
+    const bool bottom = (rho > 0.0f) == (g.s < 0.0f);
+    return (bottom ? 2 : 0) + (right ? 1 : 0);
+}
+
+// Lists the rays marked by rownorm_kernel, grouped by corner and in ray order
+// within a corner (one block, so the order and every later sum over a list
+// are deterministic): corner c's entries {k, r} sit at graze[c*capc + i] with
+// their chords in glen, i < goff[c+1] - goff[c]; goff[0..4] are the prefix
+// offsets of the flat order the SIRT forward items walk.  A line with chord
+// under 1 lies within 1/2 of the corner it clips, so a corner has at most
+// ceil(1/deltarho) + 1 such rays per angle; a ray beyond capc (not reached
+// with the caller's bound) goes back to the fast path.
+__global__ void __launch_bounds__(1024) graze_list_kernel(ProbGeom P, float *__restrict__ R, int2 *__restrict__ graze,
+                                                          float *__restrict__ glen, int *__restrict__ goff, int capc) {
+    __shared__ int s_wpos[4][32];
+    __shared__ int s_base[4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < 4) s_base[threadIdx.x] = 0;
+    __syncthreads();
+    const long long total = (long long)P.a * P.D;
+    for (long long r0 = 0; r0 < total; r0 += 1024) {
+        const long long ray = r0 + threadIdx.x;
+        int corner = -1, k = 0, r = 0;
+        if (ray < total && R[ray] < 0.0f) {
+            k = (int)(ray / P.D);
+            r = (int)(ray - (long long)k * P.D);
+            const AngleGeom g = load_geom(P.geom, k);
+            corner = graze_corner(g, __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho)));
+        }
+        unsigned m[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) m[c] = __ballot_sync(0xffffffffu, corner == c);
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) s_wpos[c][warp] = __popc(m[c]);
+        __syncthreads();
+        if (warp < 4) {
+            // exclusive scan of corner `warp`'s per-warp counts, offset by its base
+            const int v = s_wpos[warp][lane];
+            int incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int base = s_base[warp];
+            s_wpos[warp][lane] = base + incl - v;
+            __syncwarp();
+            if (lane == 31) s_base[warp] = base + incl;
+        }
+        __syncthreads();
+        if (corner >= 0) {
+            const int pos = s_wpos[corner][warp] + __popc(m[corner] & ((1u << lane) - 1u));
+            if (pos < capc) {
+                graze[(size_t)corner * capc + pos] = make_int2(k, r);
+                glen[(size_t)corner * capc + pos] = fp_ray_exact_f32<true>(P, load_geom(P.geom, k), nullptr, 0, r);
+            } else {
+                R[ray] = -R[ray];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int o = 0;
+        for (int c = 0; c < 4; ++c) {
+            goff[c] = o;
+            o += min(s_base[c], capc);
+        }
+        goff[4] = o;
+    }
 }
 
 // C = safe_inverse(A^T*1): one thread per pixel, FP64 angle sum (SIRT.fut:25).
@@ -653,10 +746,14 @@ __global__ void __launch_bounds__(256) colnorm_kernel(ProbGeom P, float *__restr
     C[(size_t)row * P.N + col] = dsum != 0.0 ? (float)(1.0 / dsum) : 0.0f;
 }
 
-cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, cudaStream_t stream) {
+cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, int2 *graze, float *glen, int *goff, int capc,
+                               cudaStream_t stream) {
     dim3 gf((P.D + 31) / 32, (P.a + 7) / 8);
     rownorm_kernel<<<gf, 256, 0, stream>>>(P, R);
     cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    graze_list_kernel<<<1, 1024, 0, stream>>>(P, R, graze, glen, goff, capc);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     dim3 gb((P.N + 31) / 32, (P.N + 7) / 8);
     colnorm_kernel<<<gb, 256, 0, stream>>>(P, C);

@@ -146,13 +146,61 @@ __device__ __forceinline__ int find_problem(const SirtParams &p, long long item,
 }
 
 // residual of one ray: e = b - fp; rr = R*e (SIRT.fut:33-36), stored times the
-// row's lbase for the SCALED backprojection; returns e^2
+// row's lbase for the SCALED backprojection; returns e^2.  A negative R marks
+// a ray that only clips a corner pixel: it is left to graze_ray (its rr stays
+// zero, so the fast backprojection adds nothing for it).
 __device__ __forceinline__ double residual(const SirtProblem &q, int s, int k, int r, float fpv) {
     const size_t pr = (size_t)q.P.a * q.P.D;
     const size_t ray = (size_t)k * q.P.D + r;
+    const float Rk = q.R[ray];
+    if (Rk < 0.0f) return 0.0;
     const float e = __fsub_rn(q.b[(size_t)s * pr + ray], fpv);
-    q.rr[(size_t)s * pr + ray] = __fmul_rn(__fmul_rn(q.R[ray], e), row_scale(q.P.geom, k));
+    q.rr[(size_t)s * pr + ray] = __fmul_rn(__fmul_rn(Rk, e), row_scale(q.P.geom, k));
     return (double)e * (double)e;
+}
+
+// Number of listed corner-clipping rays of a problem.
+__device__ __forceinline__ int graze_count(const SirtProblem &q) { return __ldg(q.goff + 4); }
+
+// Listed corner-clipping ray gidx (flat order: corner by corner) of slice s,
+// one warp; returns e^2 in lane 0.  The forward value comes from the
+// reference's row expressions over the rows the ray can touch (only the
+// corner pixel's row has a non-zero term, so the lanes' order of summation
+// gives the f32 reference's value bit for bit), and the ray's whole
+// backprojection term, chord * (R*e) as the reference forms it
+// (backprojection.fut:62-64 with SIRT.fut:35-37), is stored for its corner
+// pixel.
+__device__ __forceinline__ double graze_ray(const SirtProblem &q, int s, int gidx) {
+    int c = 0;
+    while (c < 3 && gidx >= __ldg(q.goff + c + 1)) ++c;
+    const int slot = c * q.graze_capc + (gidx - __ldg(q.goff + c));
+    const int2 ent = __ldg(q.graze + slot);
+    const int k = ent.x, r = ent.y;
+    const AngleGeom g = load_geom(q.P.geom, k);
+    const float rho = __fadd_rn(q.P.rhozero, __fmul_rn((float)r, q.P.deltarho));
+    int j0 = 0, j1 = q.P.N;
+    lane_rows(q.P, g, ray_x0(g, __fdiv_rn(rho, g.cost)), j0, j1);
+    const size_t np = (size_t)q.P.N * (q.P.N + 2);
+    const float v = fp_exact_ray_warp(q.P, k, r, q.xpad + (size_t)s * np, q.xTpad + (size_t)s * np, j0, j1);
+    double e2 = 0.0;
+    if ((threadIdx.x & 31) == 0) {
+        const size_t pr = (size_t)q.P.a * q.P.D;
+        const size_t ray = (size_t)k * q.P.D + r;
+        const float e = __fsub_rn(q.b[(size_t)s * pr + ray], v);
+        q.gcontrib[(size_t)s * 4 * q.graze_capc + slot] = __fmul_rn(__ldg(q.glen + slot), __fmul_rn(-q.R[ray], e));
+        e2 = (double)e * (double)e;
+    }
+    return e2;
+}
+
+// Backprojection terms of the listed rays that clip corner `corner` of slice
+// s, added in list order.
+__device__ __forceinline__ float corner_terms(const SirtProblem &q, int s, int corner) {
+    const int n = __ldg(q.goff + corner + 1) - __ldg(q.goff + corner);
+    const float *t = q.gcontrib + (size_t)s * 4 * q.graze_capc + (size_t)corner * q.graze_capc;
+    float acc = 0.0f;
+    for (int i = 0; i < n; ++i) acc = __fadd_rn(acc, t[i]);
+    return acc;
 }
 
 __device__ __forceinline__ void flush_e2(int it, const SirtProblem *q, int slice, SirtShared &sh) {
@@ -206,7 +254,7 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
                 for (int t = 1; t < S; ++t) fpv += sh.red[warp + t][lane];
                 e2 = residual(q, s, k, r, fpv);
             }
-        } else {
+        } else if (rem < fast_items + __ldg(q.L.counts + 2) * ((P.D + 7) / 8)) {
             const int etiles = (P.D + 7) / 8;             // near-axis rays: one per warp
             const int x = rem - fast_items;
             const int e = x / etiles;
@@ -216,6 +264,10 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
                 const float v = fp_exact_ray_warp(P, k, r, q.xpad + (size_t)s * np, q.xTpad + (size_t)s * np);
                 if (lane == 0) e2 = residual(q, s, k, r, v);
             }
+        } else {
+            // corner-clipping rays: one per warp
+            const int gidx = (rem - fast_items - __ldg(q.L.counts + 2) * ((P.D + 7) / 8)) * 8 + warp;
+            if (gidx < graze_count(q)) e2 = graze_ray(q, s, gidx);      // warp-uniform
         }
         e2 = warp_sum_d(e2);
         if (lane == 0) atomicAdd(&sh.e2, e2);
@@ -274,6 +326,9 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
                 float bpv = sh.red4[warp][m][lane];
                 for (int t = 1; t < SB; ++t) bpv += sh.red4[warp + t][m][lane];
                 const int row = row0 + RB * m;
+                // the image corners add the terms of the rays that clip only them
+                if ((row == 0 || row == P.N - 1) && (col == 0 || col == P.N - 1))
+                    bpv = __fadd_rn(bpv, corner_terms(q, s, (row == P.N - 1 ? 2 : 0) + (col == P.N - 1 ? 1 : 0)));
                 float xi = 0.0f;
                 if (row < P.N && col < P.N) {
                     const size_t pix = (size_t)row * P.N + col;
@@ -388,7 +443,9 @@ __global__ void __launch_bounds__(256) sirt_fp_stack_exact_kernel(SirtProblem q,
     if (it > q.iterations || (it == q.iterations && !record_final)) return;
     if (tol2 > 0.0 && stop_of(q, s) < it) return;
     const int nexact = __ldg(q.L.counts + 2);
-    if ((int)blockIdx.y >= nexact) return;
+    const int ngraze = graze_count(q);
+    // blocks of slot row 0 also walk the corner-clipping rays, one per warp
+    if ((int)blockIdx.y >= nexact && (blockIdx.y != 0 || ngraze == 0)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) e2s = 0.0;
     __syncthreads();
@@ -402,6 +459,8 @@ __global__ void __launch_bounds__(256) sirt_fp_stack_exact_kernel(SirtProblem q,
             if (lane == 0) e2 += residual(q, s, k, r, v);
         }
     }
+    if (blockIdx.y == 0)
+        for (int gidx = blockIdx.x * 8 + warp; gidx < ngraze; gidx += gridDim.x * 8) e2 += graze_ray(q, s, gidx);
     if (lane == 0 && e2 != 0.0) atomicAdd(&e2s, e2);
     __syncthreads();
     if (threadIdx.x == 0 && e2s != 0.0) atomicAdd(q.res2 + (size_t)s * (q.iterations + 1) + it, e2s);
@@ -439,7 +498,7 @@ __global__ void sirt_plan_kernel(SirtProblem *probs, int nprob, long long *total
         const int G = 8 / q.fp_split;
         const int ngroups = q.L.counts[0] + q.L.counts[1];
         const int nexact = q.L.counts[2];
-        q.fp_ips = ngroups * ((q.P.D + G - 1) / G) + nexact * ((q.P.D + 7) / 8);
+        q.fp_ips = ngroups * ((q.P.D + G - 1) / G) + nexact * ((q.P.D + 7) / 8) + (q.goff[4] + 7) / 8;
         const int TR = 4 * (8 / q.bp_split);
         q.bp_ips = ((q.P.N + 31) / 32) * ((q.P.N + TR - 1) / TR);
         q.fp_begin = fb;

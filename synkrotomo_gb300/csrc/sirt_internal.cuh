@@ -10,7 +10,11 @@ namespace synk {
 struct SirtProblem {
     ProbGeom P;
     AngleLists L;         // angle order of the lane-per-angle projector
-    const float *R;       // [a*D] row normaliser (shared by the slices)
+    const float *R;       // [a*D] row normaliser (shared by the slices); negative = a listed corner ray
+    const int2 *graze;    // [4*graze_capc] rays that only clip a corner pixel, {k, r}, corner c at c*graze_capc
+    const float *glen;    // [4*graze_capc] their chords (the reference's f32 sums)
+    float *gcontrib;      // [nslices][4*graze_capc] their backprojection terms chord*R*e
+    const int *goff;      // device [5]: corner c's entries are goff[c+1] - goff[c], prefix order
     const float *C;       // [N*N] column normaliser
     const float *b;       // [nslices][a*D] sinograms
     float *xpad;          // [nslices][N][N+2] iterate, zero column on each side
@@ -26,6 +30,7 @@ struct SirtProblem {
     int fp_split;         // 1,2,4,8 warps share one ray (rows split)
     int bp_split;         // 1,2,4,8 warps share one pixel (angles split)
     int bp_inrange;       // every pixel's detector window is inside the sinogram (no bounds checks)
+    int graze_capc;       // capacity of one corner's list
     // filled on the device by sirt_plan_kernel (they depend on the angle lists)
     int fp_ips;           // FP work items per slice
     int bp_ips;           // BP work items per slice

@@ -81,16 +81,50 @@ struct ProbGeom {
     float rhozero;
     float deltarho;
     float inv_deltarho;
+    // Centred detector coordinate: detector s = s' + zi sits at rz_c + s'*deltarho,
+    // rz_c = rhozero + zi*deltarho, |rz_c| <= deltarho/2.  The backprojector
+    // measures rho from rz_c rather than rhozero, so its coordinate stays below
+    // ~N/sqrt(2) in magnitude (half the rounding of one running up to D).
+    int zi;
+    float rz_c;
     const AngleGeom *geom;   // [a]
 };
 
 // Left end of a fast-path ray's segment in frame row 0, in pixel-index units:
-// u0 = intercept + min(slope,0) + half - half*slope.  Every kernel that walks a
-// ray (projectors, SIRT, CSR builders) uses this one expression with explicit
-// rounding, so all of them see bit-identical segments.
+// u0 = intercept + min(slope,0) + half - half*slope (the CSR builders' walk,
+// whose matrix and transpose are built from this one expression).
 __device__ __forceinline__ float ray_u0(const ProbGeom &P, const AngleGeom &g, float intercept) {
     const float halff = (float)P.half;
     return __fmaf_rn(-halff, g.slope, __fadd_rn(__fadd_rn(intercept, g.slope_lo), halff));
+}
+
+// Left end of a fast-path ray's segment in the centred frame, at the middle
+// row (i = j - half = 0): x0 = intercept + min(slope, 0); row j's segment
+// starts at x = (j - half)*slope + x0 and column floor(x) + half.  The
+// projectors and SIRT walk rays with it: |x| stays within ~N/2 on the rows a
+// ray crosses, so it rounds half as coarsely as the pixel-index coordinate.
+__device__ __forceinline__ float ray_x0(const AngleGeom &g, float intercept) {
+    return __fadd_rn(intercept, g.slope_lo);
+}
+
+// Frame rows [j0, j1) whose segment [x, x + |slope|] can touch a column of
+// the image, for a ray starting at x0 (ray_x0); one row of margin below and
+// two above absorb the rounding.
+__device__ __forceinline__ void ray_rows(const ProbGeom &P, const AngleGeom &g, float x0, int &j0, int &j1) {
+    j0 = 0;
+    j1 = P.N;
+    const float halff = (float)P.half;
+    const float aslope = fabsf(g.slope);
+    if (g.slope != 0.0f) {
+        const float ja = halff + (-1.0f - aslope - halff - x0) / g.slope;
+        const float jb = halff + (halff - x0) / g.slope;
+        const float lo = fmaxf(fminf(ja, jb) - 1.0f, 0.0f);
+        const float hi = fminf(fmaxf(ja, jb) + 2.0f, (float)P.N);
+        j0 = (int)lo;
+        j1 = (hi > lo) ? (int)hi : j0;
+    } else if (!(x0 > -1.0f - halff && x0 < halff)) {
+        j1 = j0;
+    }
 }
 
 // Share of the right pixel c+1 of a row segment whose left end is u, with
@@ -112,10 +146,11 @@ template <> struct FpAcc<true> { typedef double T; };
 // Rows [j0, j1) of the fast path, accumulated into (sum, comp): partial sums
 // over 32 rows, compensated across partials.
 template <bool ONES>
-__device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int N, float slope, float u0,
+__device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int N, float slope, float x0,
                                              float ainv, int j0, int j1,
                                              typename FpAcc<ONES>::T &sum, float &comp) {
     const unsigned uN = (unsigned)N;
+    const int half = N / 2;
     int j = j0;
     while (j < j1) {
         const int jend = min(j + 32, j1);
@@ -123,11 +158,12 @@ __device__ __forceinline__ void fp_rows_fast(const float *__restrict__ img, int 
         const float *row = img + (size_t)j * N;
 #pragma unroll 4
         for (; j < jend; ++j, row += N) {
-            // u = left end of the row segment in pixel-index coordinates
-            const float u = fmaf((float)j, slope, u0);
+            // x = left end of the row segment, centred; c = its pixel index
+            const float x = fmaf((float)(j - half), slope, x0);
             int c;
-            const float fl = floor_magic(u, c);
-            const float t = right_share(u, fl, ainv);                      // share of pixel c+1
+            const float fl = floor_magic(x, c);
+            c += half;
+            const float t = right_share(x, fl, ainv);                      // share of pixel c+1
             float v0, v1;
             if constexpr (ONES) {
                 v0 = ((unsigned)c < uN) ? 1.0f : 0.0f;
@@ -208,25 +244,16 @@ __device__ __forceinline__ typename FpAcc<ONES>::T fp_ray(const ProbGeom &P, con
         fp_rows_exact<ONES>(img_frame, P.N, P.half, g.slope, intercept, g.lbase, s);   // unpadded frame
         return s;
     }
-    // u(j) = xlo(row j) + half, xlo = xbot + min(slope,0), xbot = (j-half)*slope + intercept
-    const float u0 = ray_u0(P, g, intercept);
-    // rows where the segment [u, u+|slope|] can touch a pixel column in [0, N)
-    const float aslope = fabsf(g.slope);
-    int j0 = jbeg, j1 = jend;
-    if (g.slope != 0.0f) {
-        const float ja = (-1.0f - aslope - u0) / g.slope;
-        const float jb = ((float)P.N - u0) / g.slope;
-        float lo = fminf(ja, jb), hi = fmaxf(ja, jb);
-        lo = fmaxf(lo - 1.0f, (float)jbeg);
-        hi = fminf(hi + 2.0f, (float)jend);
-        j0 = (int)lo;
-        j1 = (hi > lo) ? (int)hi : j0;
-    } else if (!(u0 > -1.0f && u0 < (float)P.N)) {
-        j1 = j0;
-    }
+    // x(j) = xlo(row j) centred, xlo = xbot + min(slope,0), xbot = (j-half)*slope + intercept
+    const float x0 = ray_x0(g, intercept);
+    int j0, j1;
+    ray_rows(P, g, x0, j0, j1);
+    j0 = max(j0, jbeg);
+    j1 = min(j1, jend);
+    if (j1 < j0) j1 = j0;
     T sum = (T)0;
     float comp = 0.0f;
-    fp_rows_fast<ONES>(img_frame, P.N, g.slope, u0, g.ainv, j0, j1, sum, comp);
+    fp_rows_fast<ONES>(img_frame, P.N, g.slope, x0, g.ainv, j0, j1, sum, comp);
     if (ONES) return sum * (double)g.lbase;
     return (T)(((float)sum + comp) * g.lbase);
 }
@@ -245,11 +272,11 @@ __device__ __forceinline__ float bp_angle(const ProbGeom &P, const AngleGeom &g,
         const float yc = (float)(row - half) + 0.5f;
         const float rhoc = fmaf(xc, g.c, -yc * g.s);
         int s0;
-        ceil_magic((rhoc - fact_f32() - P.rhozero) * P.inv_deltarho, s0);
+        ceil_magic((rhoc - fact_f32() - P.rz_c) * P.inv_deltarho, s0);   // centred detector index
         float acc = 0.0f;
-        float d = fmaf((float)s0, P.deltarho, P.rhozero) - rhoc;
+        float d = fmaf((float)s0, P.deltarho, P.rz_c) - rhoc;
         for (int q = 0; q < P.rpp; ++q, d += P.deltarho) {
-            const int det = s0 + q;
+            const int det = s0 + P.zi + q;
             const float w = __saturatef(fmaf(-fabsf(d), g.inv_b, g.h_over_b));
             if ((unsigned)det < (unsigned)D) acc = fmaf(w, ONES ? 1.0f : __ldg(sino_row + det), acc);
         }
@@ -311,7 +338,11 @@ cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float2 *xpai
 // or null for the unscaled kernel (no scratch)
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
                       float *scaled);
-cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, cudaStream_t stream);
+// R, C and the lists of rays that only clip a corner pixel (their R stored
+// negated; graze [4*capc] entries {k, r} by corner, glen [4*capc] their
+// chords, goff [5] the prefix offsets; see rownorm_kernel / graze_list_kernel)
+cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, int2 *graze, float *glen, int *goff, int capc,
+                               cudaStream_t stream);
 
 // compare.cu: the validation programs (diff, mse, sanityCheck) in one pass.
 typedef synk_compare_result CompareResult;
