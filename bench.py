@@ -35,7 +35,8 @@ import numpy as np  # noqa: E402
 
 N_SIZE, N_ANGLES, N_DET = 2048, 2048, 2897     # the projector microbench's dense configuration
 METRIC = "SIRT ms to rel. residual 1e-3: warm-start vs plain, 1 GB300; FP/BP GB/s"
-LEGS = ("proj", "e2e", "sirt", "csr", "unet", "cpu")   # default legs; "batch", "stack", "sparse" on request
+LEGS = ("proj", "e2e", "sirt", "csr", "unet", "warm", "shard", "cpu")   # default legs; "batch", "stack", "sparse" on request
+WARM_CHECKPOINT = os.path.join(ROOT, "synkrotomo_gb300", "checkpoints", "unet_n256_a180_noisefree.npz")
 
 
 def set_workload(size, angles, detectors):
@@ -300,7 +301,9 @@ def run_gpu(args, rank, world):
     stack = run_stack_cfg2(dev) if (rank == 0 and "stack" in args.legs) else None
     sparse = run_sparseview(dev) if (rank == 0 and "sparse" in args.legs) else None
     unet = run_unet(dev) if (rank == 0 and "unet" in args.legs) else None
-    return {"sparse": sparse, "unet": unet, "step_ms": step_ms, "fp_ms": statistics.median(fp_ms), "bp_ms": statistics.median(bp_ms),
+    warm = run_warm(dev) if (rank == 0 and "warm" in args.legs) else None
+    shardleg = run_sirt3d_sharded(dev, world) if "shard" in args.legs else None
+    return {"sparse": sparse, "unet": unet, "warm": warm, "shard": shardleg, "step_ms": step_ms, "fp_ms": statistics.median(fp_ms), "bp_ms": statistics.median(bp_ms),
             "wall_s": wall, "clocks": clk.summary(), "e2e": e2e, "sirt": sirt, "csr": csr, "batch": batch,
             "stack": stack,
             "sms": torch.cuda.get_device_properties(dev).multi_processor_count}
@@ -371,6 +374,47 @@ def run_sirt_cfg0(dev):
         out[label] = {"ms": statistics.median(ts), "iterations": int(done.item())}
     out["target_residual"] = target
     return out
+
+
+def run_sirt3d_sharded(dev, world, slices_per_rank=8, iterations=20, seed=0):
+    """The slice stack's geometry (512 x 512 slices, 360 angles, 725
+    detectors, 1 % noise) split over the ranks by shard.sirt3d_sharded
+    (contiguous slice ranges, one SIRT launch per rank, one all-gather of the
+    results at the end): slices_per_rank slices per rank (weak scaling),
+    iterations updates each.  Returns the slowest rank's milliseconds and the
+    whole job's slice-iterations per second."""
+    import torch
+
+    from synkrotomo_gb300 import phantom, shard
+    from synkrotomo_gb300 import runtime as rt
+
+    N, a, D = 512, 360, 725
+    ns = slices_per_rank * world
+    g = phantom.geometry(N, a, numrhos=D)
+    ang = torch.from_numpy(g.angles).to(dev)
+    rhos = torch.from_numpy((np.float32(g.rhozero) + np.arange(D, dtype=np.float32)).astype(np.float32)).to(dev)
+    vol = phantom.ellipsoid_volume(N, ns, seed)
+    sinos = []
+    for z in range(ns):     # every rank makes the same stack (same seeds)
+        b = rt.forwardprojection(ang, g.rhozero, g.deltarho, D, torch.from_numpy(vol[z]).to(dev))
+        gen = torch.Generator(device=dev).manual_seed(seed * 1000 + z)
+        sinos.append(b + torch.randn(b.shape, device=dev, generator=gen) * (0.01 * float(b.max())))
+    proj = torch.cat(sinos)
+    shard.sirt3d_sharded(ang, rhos, proj, 2, N, nslices=ns)          # warm-up
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    volr = shard.sirt3d_sharded(ang, rhos, proj, iterations, N, nslices=ns)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = shard.max_over_ranks(e0.elapsed_time(e1))
+    assert volr.numel() == ns * N * N
+    return {"slices": ns, "slices_per_rank": slices_per_rank, "iterations": iterations, "ranks": world,
+            "ms": ms, "slice_iterations_per_s": ns * iterations / (ms * 1e-3),
+            "split": "contiguous slice ranges, one all-gather of the results"}
 
 
 def run_csr_cfg1(dev, reps=20):
@@ -531,6 +575,28 @@ def run_sparseview(dev, size=512, detectors=725, counts=(1, 5, 10, 20, 30, 45, 6
     return {"size": size, "detectors": detectors, "angles": out}
 
 
+def run_warm(dev, n=64, per_image=16, tol=1e-3, max_iters=8000):
+    """The headline comparison: milliseconds and iterations to relative
+    residual 1e-3, plain zero-start SIRT against warm-started SIRT
+    (warmstart.solve), on 64 held-out noise-free phantoms at N=256, 180
+    angles, 363 detectors; the network is the committed checkpoint that this
+    library trained on GPU-made pairs (its metadata is reported)."""
+    import torch
+
+    from synkrotomo_gb300 import warmstart
+    from synkrotomo_gb300.unet import UNet
+    if not os.path.exists(WARM_CHECKPOINT):
+        return {"unavailable": f"checkpoint {os.path.relpath(WARM_CHECKPOINT, ROOT)} not found"}
+    net = UNet(256, 32, seed=0)
+    meta = net.load_checkpoint(WARM_CHECKPOINT)
+    prob = warmstart.Problem(256, 180, noise=0.0)
+    out = warmstart.headline(net, prob, n=n, seed=777777, tol=tol, max_iters=max_iters, per_image=per_image)
+    out["checkpoint"] = {"file": os.path.relpath(WARM_CHECKPOINT, ROOT), **meta}
+    del net
+    torch.cuda.synchronize()
+    return out
+
+
 def unet_flops(size, batch):
     """Tensor-core FLOPs of one U-Net training step (2*H*W*Cin*Cout*9 per 3x3
     conv and pass): forward, backward-data and backward-weights of the 13
@@ -689,6 +755,10 @@ def main():
         u["frac_forward_of_measured_bf16"] = u["tflops_forward"] / bf16
         u["bf16_peak_tflops"] = bf16
         line["unet_cfg4"] = u
+    if res["warm"] is not None:
+        line["warm_start"] = res["warm"]
+    if res["shard"] is not None:
+        line["sirt3d_sharded"] = res["shard"]
     if "cpu" in args.legs:
         if "sirt_cfg0" in line:
             c0 = cpu_sirt_cfg0()

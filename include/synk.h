@@ -289,6 +289,12 @@ void synk_unet_free(synk_unet *net);
 int64_t synk_unet_num_params(const synk_unet *net);
 /* direction 0: copy the FP32 parameters to dst; 1: load them from dst. */
 int synk_unet_params(synk_context *ctx, synk_unet *net, float *dst, int32_t direction);
+/* Adam state, for checkpoints: direction 0 copies the first and second
+ * moments to the DEVICE arrays m and v ([num_params] FP32 each, the parameter
+ * layout) and the number of Adam steps taken to the HOST scalar *step;
+ * direction 1 loads all three, so that training resumes where it stopped. */
+int synk_unet_optimizer_state(synk_context *ctx, synk_unet *net, float *m, float *v, int64_t *step,
+                              int32_t direction);
 /* y = net(x) for `batch` images. */
 int synk_unet_forward(synk_context *ctx, synk_unet *net, const float *x, float *y, int32_t batch);
 /* One training step on (x, target) with the MSE loss: forward, backward and,

@@ -120,6 +120,8 @@ SIGNATURES = {
     "synk_unet_free": (None, [ctypes.c_void_p]),
     "synk_unet_num_params": (ctypes.c_int64, [ctypes.c_void_p]),
     "synk_unet_params": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "synk_unet_optimizer_state": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]),
     "synk_unet_forward": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "synk_unet_train_step": (ctypes.c_int, [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                             ctypes.c_float, ctypes.c_int32, ctypes.c_void_p]),

@@ -820,6 +820,27 @@ int synk_unet_params(synk_context *ctx, synk_unet *net, float *dst, int32_t dire
     return SYNK_OK;
 }
 
+int synk_unet_optimizer_state(synk_context *ctx, synk_unet *net, float *m, float *v, int64_t *step,
+                              int32_t direction) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!net || !m || !v || !step) return fail(ctx, SYNK_EINVAL, "null pointer");
+    if (direction != 0 && direction != 1) return fail(ctx, SYNK_EINVAL, "direction must be 0 or 1 (got %d)", direction);
+    const size_t bytes = sizeof(float) * (size_t)unet::net_nparams(net->net);
+    int *st = unet::net_adam_step(net->net);
+    if (direction == 0) {
+        SYNK_CUDA(cudaMemcpyAsync(m, unet::net_adam_m(net->net), bytes, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        SYNK_CUDA(cudaMemcpyAsync(v, unet::net_adam_v(net->net), bytes, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        *step = *st;
+    } else {
+        if (*step < 0 || *step > INT32_MAX) return fail(ctx, SYNK_EINVAL, "Adam step %lld out of range", (long long)*step);
+        SYNK_CUDA(cudaMemcpyAsync(unet::net_adam_m(net->net), m, bytes, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        SYNK_CUDA(cudaMemcpyAsync(unet::net_adam_v(net->net), v, bytes, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        *st = (int)*step;
+    }
+    return SYNK_OK;
+}
+
 int synk_unet_forward(synk_context *ctx, synk_unet *net, const float *x, float *y, int32_t batch) {
     int rc = check_ctx(ctx);
     if (rc) return rc;

@@ -199,7 +199,13 @@ __device__ __forceinline__ float corner_terms(const SirtProblem &q, int s, int c
     const int n = __ldg(q.goff + corner + 1) - __ldg(q.goff + corner);
     const float *t = q.gcontrib + (size_t)s * 4 * q.graze_capc + (size_t)corner * q.graze_capc;
     float acc = 0.0f;
-    for (int i = 0; i < n; ++i) acc = __fadd_rn(acc, t[i]);
+    for (int i0 = 0; i0 < n; i0 += 8) {
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = i0 + j < n ? t[i0 + j] : 0.0f;   // loads in flight together
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc = __fadd_rn(acc, v[j]);             // acc + 0 is acc
+    }
     return acc;
 }
 

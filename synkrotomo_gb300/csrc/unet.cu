@@ -187,6 +187,9 @@ void net_free(Net *n) { delete n; }
 long long net_nparams(const Net *n) { return n->nparams; }
 float *net_params(Net *n) { return n->params; }
 float *net_grads(Net *n) { return n->grads; }
+float *net_adam_m(Net *n) { return n->m; }
+float *net_adam_v(Net *n) { return n->v; }
+int *net_adam_step(Net *n) { return &n->step; }
 
 cudaError_t net_refresh_weights(Net *n, cudaStream_t st) {
     for (int l = 1; l < 14; ++l) {

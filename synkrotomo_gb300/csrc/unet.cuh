@@ -14,6 +14,9 @@ void net_free(Net *n);
 long long net_nparams(const Net *n);
 float *net_params(Net *n);   // device, FP32 [nparams]: per layer w [cout][9*cin] then b [cout]; head w [32], b
 float *net_grads(Net *n);    // device, FP32 [nparams], same layout
+float *net_adam_m(Net *n);   // device, FP32 [nparams]: Adam first moments
+float *net_adam_v(Net *n);   // device, FP32 [nparams]: Adam second moments
+int *net_adam_step(Net *n);  // host: Adam steps taken (bias correction)
 double *net_loss(Net *n);    // device, the last forward's MSE
 cudaError_t net_refresh_weights(Net *n, cudaStream_t st);
 // y (optional) [B][N][N] = net(x); with target, the MSE goes to net_loss and

@@ -184,21 +184,25 @@ def _gpu_slices(angles, rhos, projections, iterations, size, nslices):
 
 
 def sirt3d_sharded(angles, rhos, projections, iterations: int, size: int, solve: Callable | None = None,
-                   group=None) -> torch.Tensor:
-    """SIRT3D (``size`` slices of ``size``x``size``) with the slices split
-    over the ranks; every rank returns the whole volume.
+                   group=None, nslices: int | None = None) -> torch.Tensor:
+    """SIRT3D (``size`` slices of ``size``x``size``, or ``nslices`` slices
+    for a non-cubic stack) with the slices split over the ranks; every rank
+    returns the whole volume.
 
     ``solve(angles, rhos, projections_part, iterations, size, nslices)``
     reconstructs a contiguous run of slices (default: this rank's GPU)."""
     world, rank = world_rank(group)
     solve = solve or _gpu_slices
     a, r = int(angles.numel()), int(rhos.numel())
+    ns = int(size) if nslices is None else int(nslices)
+    if ns < 1:
+        raise ValueError(f"nslices must be positive (got {ns})")
     if r < 2:
         raise ValueError(f"rhos needs at least two detector positions (got {r})")
     per = a * r
-    if projections.numel() != int(size) * per:
-        raise ValueError(f"projections has {projections.numel()} values, expected size*a*r = {int(size) * per}")
-    ranges = slice_ranges(int(size), world)
+    if projections.numel() != ns * per:
+        raise ValueError(f"projections has {projections.numel()} values, expected slices*a*r = {ns * per}")
+    ranges = slice_ranges(ns, world)
     owner = [k for k, (s0, s1) in enumerate(ranges) for _ in range(s0, s1)]
     s0, s1 = ranges[rank]
     n2 = int(size) * int(size)

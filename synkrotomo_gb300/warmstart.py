@@ -23,6 +23,7 @@ import json
 import math
 import time
 
+import numpy as np
 import torch
 
 from . import phantom
@@ -131,6 +132,118 @@ def train(net: UNet, inputs: torch.Tensor, targets: torch.Tensor, epochs: int, b
         if log:
             log(f"epoch {ep}: loss {ep_loss:.6g}")
     return hist
+
+
+class WarmResult:
+    """Result of ``solve``: images x [n, N*N], updates applied [n], the
+    residual of the network's start [n], which images fell back to the zero
+    start [n], and optionally the residual histories [n, max_iters+1]."""
+
+    def __init__(self, x, iterations, start_residual, fallback, residuals=None):
+        self.x, self.iterations, self.start_residual = x, iterations, start_residual
+        self.fallback, self.residuals = fallback, residuals
+
+
+def solve(net: UNet, angles, rhozero: float, deltarho: float, sinograms, tol: float = 1e-3,
+          max_iters: int = 8000, residuals: bool = False) -> WarmResult:
+    """Warm-started SIRT of one or more sinograms of one geometry.
+
+    ``sinograms``: one flat sinogram [a*numrhos] or a batch [n, a*numrhos]
+    (float32; numpy or torch); numrhos = length / a, as SIRT.fut:18 derives
+    it; the image side is the network's.  Steps, all on the GPU with no host
+    round trip:
+      1. x1 = one SIRT update from zero (C*A^T*R*b, the network's input);
+      2. x0 = net(x1);
+      3. the relative data residual ||A x0 - b|| / ||b|| of each start; where
+         it exceeds the zero start's (1.0), that image starts from zero
+         instead (the fallback);
+      4. SIRT from x0 until the residual is at most ``tol`` or ``max_iters``
+         updates (x <- x + C*A^T*R*(b - A*x), SIRT.fut:27-39; the start image
+         plays the role of SIRT.fut:12's ``image``).
+    """
+    ang = rt.to_device_f32(angles, 0, "angles")
+    b = sinograms if isinstance(sinograms, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(sinograms))
+    if b.dtype != torch.float32:
+        raise TypeError(f"sinograms must be float32 (got {b.dtype})")
+    b = b.to(ang.device)
+    if b.dim() == 1:
+        b = b.view(1, -1)
+    if b.dim() != 2:
+        raise ValueError(f"sinograms must be [a*numrhos] or [n, a*numrhos] (got shape {tuple(b.shape)})")
+    n, p = b.shape
+    a = ang.numel()
+    if a < 1 or p % a:
+        raise ValueError(f"sinogram length {p} is not a multiple of {a} angles")
+    numrhos = p // a
+    N = net.size
+    b = b.contiguous().view(-1)
+    x1, _, _ = rt.sirt_slices(ang, rhozero, deltarho, numrhos, N, n, None, b, 1)
+    x0 = net.forward(x1.view(n, N, N)).view(n, N * N)
+    _, r0, _ = rt.sirt_slices(ang, rhozero, deltarho, numrhos, N, n, x0.view(-1), b, 0, residuals=True)
+    start_res = r0[:, 0]
+    fallback = ~(start_res <= 1.0)          # NaN falls back too
+    x0 = torch.where(fallback[:, None], torch.zeros_like(x0), x0)
+    x, res, done = rt.sirt_slices(ang, rhozero, deltarho, numrhos, N, n, x0.view(-1), b, int(max_iters),
+                                  tol=float(tol), residuals=residuals)
+    return WarmResult(x.view(n, N * N), done, start_res, fallback, res)
+
+
+def headline(net: UNet, prob: "Problem", n: int = 64, seed: int = 777777, tol: float = 1e-3,
+             max_iters: int = 8000, per_image: int = 16) -> dict:
+    """Milliseconds and iterations to the relative residual ``tol``: plain
+    zero-start SIRT against ``solve`` on n held-out seeded phantoms (the
+    problem's geometry and noise), all n in one call each way, and the first
+    ``per_image`` images solved one call each.  Every timed region is CUDA
+    events on the current stream after one untimed run of the same call; the
+    warm side includes the SIRT update that makes the network's input, the
+    network and the fallback check."""
+    g = prob.g
+    imgs = ellipse_batch(n, prob.size, seed)
+    b = prob.sinograms(imgs, seed)
+
+    def plain(bs):
+        return rt.sirt_slices(prob.angles, g.rhozero, g.deltarho, g.numrhos, prob.size, bs.shape[0], None,
+                              bs.reshape(-1).contiguous(), max_iters, tol=tol)[2]
+
+    def warm(bs):
+        r = solve(net, prob.angles, g.rhozero, g.deltarho, bs, tol=tol, max_iters=max_iters)
+        return r.iterations, r.fallback
+
+    def timed(fn, bs):
+        fn(bs)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn(bs)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    ms_plain, it_plain = timed(plain, b)
+    ms_warm, (it_warm, fb) = timed(warm, b)
+    pi_plain = pi_warm = 0.0
+    ratios = []
+    k = min(per_image, n)
+    for i in range(k):
+        tp, _ = timed(plain, b[i:i + 1])
+        tw, _ = timed(warm, b[i:i + 1])
+        pi_plain += tp
+        pi_warm += tw
+        ratios.append(tp / max(tw, 1e-9))
+    it_plain = it_plain.float().cpu()
+    it_warm = it_warm.float().cpu()
+    return {"images": n, "size": prob.size, "angles": prob.n_angles, "noise": prob.noise, "target_residual": tol,
+            "max_iterations": max_iters,
+            "plain_iterations_mean": float(it_plain.mean()), "plain_iterations_median": float(it_plain.median()),
+            "warm_iterations_mean": float(it_warm.mean()), "warm_iterations_median": float(it_warm.median()),
+            "plain_not_reached": int((it_plain >= max_iters).sum()),
+            "warm_not_reached": int((it_warm >= max_iters).sum()),
+            "fallback_images": int(fb.sum().item()),
+            "median_iteration_ratio": float(torch.median(it_plain / it_warm.clamp(min=1.0))),
+            "batched_ms_plain": ms_plain, "batched_ms_warm": ms_warm, "speedup_batched": ms_plain / ms_warm,
+            "per_image_images": k, "per_image_ms_plain": pi_plain, "per_image_ms_warm": pi_warm,
+            "speedup_per_image": pi_plain / max(pi_warm, 1e-9),
+            "speedup_per_image_median": float(torch.tensor(ratios).median()) if ratios else None}
 
 
 def first_below(hist: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
@@ -254,6 +367,9 @@ def main(argv=None):
     ap.add_argument("--sparse-size", type=int, default=512)
     ap.add_argument("--sparse-angles", type=int, default=90)
     ap.add_argument("--out", default="")
+    ap.add_argument("--save", default="", help="write the trained network as an inference checkpoint (.npz)")
+    ap.add_argument("--save-full", default="", help="write weights and Adam state (.npz, resumable)")
+    ap.add_argument("--skip-eval", action="store_true")
     args = ap.parse_args(argv)
     torch.cuda.set_device(0)
     log = lambda m: print(m, flush=True)   # noqa: E731
@@ -281,11 +397,24 @@ def main(argv=None):
     torch.cuda.synchronize()
     t_train = time.time() - t0
     del xs, ts
+    meta = {"phantoms": args.train, "noise": args.noise, "target_iters": args.target_iters, "size": args.size,
+            "angles": args.angles, "mix_angles": args.mix_angles, "epochs": args.epochs, "batch": args.batch,
+            "lr": args.lr, "final_loss": hist[-1] if hist else None, "data_seed": 1, "init_seed": 0,
+            "train_s": t_train, "data_s": t_data}
+    if args.save:
+        net.save(args.save, meta=meta, compact=True)
+    if args.save_full:
+        net.save(args.save_full, meta=meta, optimizer=True)
     res = {"train": {"phantoms": args.train, "noise": args.noise, "target_iters": args.target_iters,
                      "angles": args.angles, "mix_angles": args.mix_angles, "epochs": args.epochs, "batch": args.batch,
                      "lr": args.lr,
                      "loss_per_epoch": hist, "data_s": t_data, "train_s": t_train,
                      "steps": args.epochs * (args.train // args.batch)}}
+    if args.skip_eval:
+        if args.out:
+            with open(args.out, "w") as f:
+                json.dump(res, f, indent=1)
+        return res
     res["eval_dense"] = evaluate(net, prob, args.eval, seed=777777, budgets=budgets, max_iters=args.max_iters,
                                  abs_targets=abs_t)
     log(json.dumps(res["eval_dense"]))

@@ -242,3 +242,18 @@ def test_a_local_fault_on_one_rank_fails_every_rank(fault, kind):
             if p.is_alive():
                 p.kill()
     assert got == {0: kind, 1: kind}
+
+
+def test_sirt3d_sharded_non_cubic_stack_single_rank():
+    """nslices != size: a stack of 3 slices of 10 x 10 through the driver
+    equals the oracle's stack."""
+    ang, rhos, _, it, size = _sirt3d_case()
+    rng = np.random.default_rng(11)
+    stack = rng.random(3 * ang.size * rhos.size).astype(np.float32)
+    vol = shard.sirt3d_sharded(torch.from_numpy(ang), torch.from_numpy(rhos), torch.from_numpy(stack), it, size,
+                               solve=_cpu_slices, nslices=3)
+    ref = cpu_ref.sirt3d(ang, rhos, stack, it, size, nslices=3)
+    np.testing.assert_array_equal(vol.numpy(), ref)
+    with pytest.raises(ValueError):
+        shard.sirt3d_sharded(torch.from_numpy(ang), torch.from_numpy(rhos), torch.from_numpy(stack), it, size,
+                             solve=_cpu_slices, nslices=4)
