@@ -340,8 +340,9 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         AngleGeom *geom;
         float *R, *C, *xpad, *xTpad, *rr, *glen, *gcontrib;
         double *res2, *b2;
-        int *stop_iter, *goff;
-        int2 *graze;
+        int *stop_iter, *goff, *gcnt;
+        int2 *graze, *graze_tmp;
+        float *glen_tmp;
         // rays that only clip a corner pixel: per corner and angle at most
         // ceil(1/deltarho) + 1 (graze_list_kernel)
         const double gcapc = (double)q.a * (ceil(1.0 / (double)q.deltarho) + 1.0);
@@ -351,6 +352,9 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         SYNK_CUDA(sc.get(&glen, 4 * (size_t)graze_capc), "cudaMallocAsync");
         SYNK_CUDA(sc.get(&gcontrib, 4 * (size_t)graze_capc * q.nslices), "cudaMallocAsync");
         SYNK_CUDA(sc.get(&goff, 5), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&graze_tmp, 4 * (size_t)graze_capc), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&glen_tmp, 4 * (size_t)graze_capc), "cudaMallocAsync");
+        SYNK_CUDA(sc.get(&gcnt, 4), "cudaMallocAsync");
         SYNK_CUDA(sc.get(&R, pr), "cudaMallocAsync(R)");
         SYNK_CUDA(sc.get(&C, n), "cudaMallocAsync(C)");
         SYNK_CUDA(sc.get(&xpad, np * q.nslices), "cudaMallocAsync(padded image)");
@@ -365,7 +369,8 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         SYNK_CUDA(cudaGetLastError(), "fill kernel");
         h.P = make_geom(q.a, q.rhozero, q.deltarho, q.numrhos, q.size, geom);
         SYNK_CUDA(make_setup(sc, q.angles, h.P, &h.L, st), "setup kernel");
-        SYNK_CUDA(launch_normalisers(h.P, R, C, graze, glen, goff, graze_capc, st), "normaliser kernels");
+        SYNK_CUDA(launch_normalisers(h.P, R, C, graze, glen, goff, graze_tmp, glen_tmp, gcnt, graze_capc, st),
+                  "normaliser kernels");
         // the listed rays' entries stay zero (their terms go to the corner pixels)
         SYNK_CUDA(cudaMemsetAsync(rr, 0, sizeof(float) * pr * q.nslices, st), "memset");
         SYNK_CUDA(launch_pad(q.out, xpad, xTpad, q.size, q.nslices, st), "pad kernel");

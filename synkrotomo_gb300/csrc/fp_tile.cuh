@@ -83,16 +83,19 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
     const int stride = P.N + 2;
     const unsigned lim = (unsigned)P.N;     // c + 1 in [0, N]
     const int half = P.half;
-    const float *img_c = img_pad + half + 1;   // centred column 0 of frame row 0
+    // floor(x) + half straight from the bits: x + (kMagic + half) rounded down
+    // holds it in the low mantissa bits (kMagic + half is an exact float)
+    const float magic_h = kMagic + (float)half;
     // x of rows j..j+3 from one float row counter: x0 + k*slope per lane
     const float x1 = x0 + slope, x2 = x0 + 2.0f * slope, x3 = x0 + 3.0f * slope;
     float sum = 0.0f, comp = 0.0f;
     auto row = [&](float x, int jrow, float &part) {
-        int c;                                  // centred column
-        const float fl = floor_magic(x, c);
+        const float rr = __fadd_rd(x, magic_h);
+        const int c = __float_as_int(rr) - kMagicBits;     // pixel index floor(x) + half
+        const float fl = __fsub_rn(rr, magic_h);             // floor(x)
         const float t = right_share(x, fl, ainv);
-        const bool ok = (unsigned)(c + half + 1) <= lim;
-        const float *p = img_c + (jrow * stride + c);
+        const bool ok = (unsigned)(c + 1) <= lim;
+        const float *p = img_pad + (jrow * stride + c + 1);
         const float v0 = ok ? __ldg(p) : 0.0f;
         const float v1 = ok ? __ldg(p + 1) : 0.0f;
         part += fmaf(t, v1 - v0, v0);

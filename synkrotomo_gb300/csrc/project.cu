@@ -12,6 +12,7 @@
 //             bp_split_kernel  the same with the angles split over warps (images too small
 //                              for one block per tile to fill the GPU)
 // See fp_tile.cuh and bp_tile.cuh for the per-ray and per-pixel arithmetic.
+#include <limits.h>
 #include <math.h>
 
 #include "synk_internal.cuh"
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_tile_kern
         float part[kBpPix];
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) part[m] = 0.0f;
-        bp_chunk<kBpPix, UNIT, INRANGE, SCALED>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
+        bp_chunk<kBpPix, UNIT, INRANGE, SCALED, 2>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) comp_add(sum[m], comp[m], part[m]);
     }
@@ -559,7 +560,7 @@ __global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_split_ker
         float prt[kBpPix];
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) prt[m] = 0.0f;
-        bp_chunk<kBpPix, UNIT, INRANGE, SCALED>(P, st, kc, P.a, part, SB, sino_s, xc, yc0, (float)RB, prt);
+        bp_chunk<kBpPix, UNIT, INRANGE, SCALED, 2>(P, st, kc, P.a, part, SB, sino_s, xc, yc0, (float)RB, prt);
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) comp_add(sum[m], comp[m], prt[m]);
     }
@@ -627,10 +628,30 @@ cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino,
 
 // ---- normalisers (FP64 sums) -----------------------------------------------------------
 
+// The corner pixel a ray that only clips a corner cuts: the corner of the
+// image square with the extreme rho = x cos - y sin on the ray's side
+// (x = +-half at columns N-1 / 0, y = +-half at rows N-1 / 0); 0: row 0 col 0,
+// 1: row 0 col N-1, 2: row N-1 col 0, 3: row N-1 col N-1.
+__device__ __forceinline__ int graze_corner(const AngleGeom &g, float rho) {
+    const bool right = (rho > 0.0f) == (g.c > 0.0f);
+    const bool bottom = (rho > 0.0f) == (g.s < 0.0f);
+    return (bottom ? 2 : 0) + (right ? 1 : 0);
+}
+
 // R = safe_inverse(A*1): one thread per ray (SIRT.fut:22-23, sirtlib.fut:9-13).
-// R is stored negated for the rays that only clip a corner pixel (see below);
-// graze_list_kernel lists them and the SIRT phases read the sign.
-__global__ void __launch_bounds__(256) rownorm_kernel(ProbGeom P, float *__restrict__ R) {
+// A ray whose chord is under 1 cuts off a corner of the image inside one
+// corner pixel.  There R = 1/chord magnifies the chord's rounding (the fast
+// row rule and the backprojector's trapezoid differ by up to a few per cent
+// on such rays), so the chord is the reference's own f32 sum
+// (forwardprojection.fut:31-56), which equals the reference's backprojection
+// weight for that pixel bit for bit.  Such a ray (of a fast-path angle;
+// near-axis angles take the exact path anyway) is appended to its corner's
+// list (graze, glen: unsorted, slots taken by atomics; graze_sort_kernel
+// orders them) and its R is stored negated, which sends it to the SIRT
+// kernels' exact treatment (sirt.cu).  A ray without a slot (not reached with
+// the caller's bound) keeps the fast path.
+__global__ void __launch_bounds__(256) rownorm_kernel(ProbGeom P, float *__restrict__ R, int2 *__restrict__ graze,
+                                                      float *__restrict__ glen, int *__restrict__ gcnt, int capc) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k = blockIdx.y * 8 + warp;
     const int r = blockIdx.x * 32 + lane;
@@ -639,93 +660,57 @@ __global__ void __launch_bounds__(256) rownorm_kernel(ProbGeom P, float *__restr
     const double v = fp_ray<true>(P, g, nullptr, r, 0, P.N);
     float Rv = v != 0.0 ? (float)(1.0 / v) : 0.0f;
     if (v > 0.0 && v < 1.0 && !g.exact) {
-        // A chord under 1 cuts off a corner of the image inside one corner
-        // pixel.  There R = 1/chord magnifies the chord's rounding (the fast
-        // row rule and the backprojector's trapezoid differ by up to a few
-        // per cent on such rays), so the chord is the reference's own f32 sum
-        // (sirtlib.fut:9-13 inverse of forwardprojection.fut:31-56), which
-        // equals the reference's backprojection weight for that pixel bit for
-        // bit.  The sign sends the ray to the SIRT kernels' exact treatment
-        // (sirt.cu); near-axis angles already take the exact path.
         const float e = fp_ray_exact_f32<true>(P, g, nullptr, 0, r);
-        if (e != 0.0f) Rv = -__fdiv_rn(1.0f, e);
+        if (e != 0.0f) {
+            const int c = graze_corner(g, __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho)));
+            const int slot = atomicAdd(gcnt + c, 1);
+            if (slot < capc) {
+                graze[(size_t)c * capc + slot] = make_int2(k, r);
+                glen[(size_t)c * capc + slot] = e;
+                Rv = -__fdiv_rn(1.0f, e);
+            }
+        }
     }
     R[(size_t)k * P.D + r] = Rv;
 }
 
-// The corner pixel a listed ray clips: the corner of the image square with
-// the extreme rho = x cos - y sin on the ray's side (x = +-half at columns
-// N-1 / 0, y = +-half at rows N-1 / 0); 0: row 0 col 0, 1: row 0 col N-1,
-// 2: row N-1 col 0, 3: row N-1 col N-1.
-__device__ __forceinline__ int graze_corner(const AngleGeom &g, float rho) {
-    const bool right = (rho > 0.0f) == (g.c > 0.0f);
-    const bool bottom = (rho > 0.0f) == (g.s < 0.0f);
-    return (bottom ? 2 : 0) + (right ? 1 : 0);
-}
-
-// Lists the rays marked by rownorm_kernel, grouped by corner and in ray order
-// within a corner (one block, so the order and every later sum over a list
-// are deterministic): corner c's entries {k, r} sit at graze[c*capc + i] with
-// their chords in glen, i < goff[c+1] - goff[c]; goff[0..4] are the prefix
-// offsets of the flat order the SIRT forward items walk.  A line with chord
-// under 1 lies within 1/2 of the corner it clips, so a corner has at most
-// ceil(1/deltarho) + 1 such rays per angle; a ray beyond capc (not reached
-// with the caller's bound) goes back to the fast path.
-__global__ void __launch_bounds__(1024) graze_list_kernel(ProbGeom P, float *__restrict__ R, int2 *__restrict__ graze,
+// Orders each corner's list by ray (k, r) -- one block; a rank sort, each
+// entry's position being the number of smaller keys -- into graze/glen, so
+// every later sum over a list is deterministic; goff[0..4] are the prefix
+// offsets of the flat order the SIRT forward items walk (corner c holds
+// goff[c+1] - goff[c] entries).
+__global__ void __launch_bounds__(1024) graze_sort_kernel(const int2 *__restrict__ ug, const float *__restrict__ ul,
+                                                          const int *__restrict__ gcnt, int2 *__restrict__ graze,
                                                           float *__restrict__ glen, int *__restrict__ goff, int capc) {
-    __shared__ int s_wpos[4][32];
-    __shared__ int s_base[4];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x < 4) s_base[threadIdx.x] = 0;
-    __syncthreads();
-    const long long total = (long long)P.a * P.D;
-    for (long long r0 = 0; r0 < total; r0 += 1024) {
-        const long long ray = r0 + threadIdx.x;
-        int corner = -1, k = 0, r = 0;
-        if (ray < total && R[ray] < 0.0f) {
-            k = (int)(ray / P.D);
-            r = (int)(ray - (long long)k * P.D);
-            const AngleGeom g = load_geom(P.geom, k);
-            corner = graze_corner(g, __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho)));
-        }
-        unsigned m[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) m[c] = __ballot_sync(0xffffffffu, corner == c);
-        if (lane == 0)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) s_wpos[c][warp] = __popc(m[c]);
-        __syncthreads();
-        if (warp < 4) {
-            // exclusive scan of corner `warp`'s per-warp counts, offset by its base
-            const int v = s_wpos[warp][lane];
-            int incl = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
+    __shared__ int2 sh[1024];
+    for (int c = 0; c < 4; ++c) {
+        const int n = min(gcnt[c], capc);                  // block-uniform
+        const int2 *u = ug + (size_t)c * capc;
+        for (int i0 = 0; i0 < n; i0 += 1024) {
+            const int i = i0 + (int)threadIdx.x;
+            const int2 me = i < n ? u[i] : make_int2(INT_MAX, INT_MAX);
+            int rank = 0;
+            for (int j0 = 0; j0 < n; j0 += 1024) {
+                __syncthreads();
+                if (j0 + (int)threadIdx.x < n) sh[threadIdx.x] = u[j0 + threadIdx.x];
+                __syncthreads();
+                const int m = min(1024, n - j0);
+                for (int j = 0; j < m; ++j) {
+                    const int2 o = sh[j];
+                    rank += (o.x < me.x || (o.x == me.x && o.y < me.y)) ? 1 : 0;
+                }
             }
-            const int base = s_base[warp];
-            s_wpos[warp][lane] = base + incl - v;
-            __syncwarp();
-            if (lane == 31) s_base[warp] = base + incl;
-        }
-        __syncthreads();
-        if (corner >= 0) {
-            const int pos = s_wpos[corner][warp] + __popc(m[corner] & ((1u << lane) - 1u));
-            if (pos < capc) {
-                graze[(size_t)corner * capc + pos] = make_int2(k, r);
-                glen[(size_t)corner * capc + pos] = fp_ray_exact_f32<true>(P, load_geom(P.geom, k), nullptr, 0, r);
-            } else {
-                R[ray] = -R[ray];
+            if (i < n) {
+                graze[(size_t)c * capc + rank] = me;
+                glen[(size_t)c * capc + rank] = ul[(size_t)c * capc + i];
             }
         }
-        __syncthreads();
     }
     if (threadIdx.x == 0) {
         int o = 0;
         for (int c = 0; c < 4; ++c) {
             goff[c] = o;
-            o += min(s_base[c], capc);
+            o += min(gcnt[c], capc);
         }
         goff[4] = o;
     }
@@ -746,13 +731,15 @@ __global__ void __launch_bounds__(256) colnorm_kernel(ProbGeom P, float *__restr
     C[(size_t)row * P.N + col] = dsum != 0.0 ? (float)(1.0 / dsum) : 0.0f;
 }
 
-cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, int2 *graze, float *glen, int *goff, int capc,
-                               cudaStream_t stream) {
-    dim3 gf((P.D + 31) / 32, (P.a + 7) / 8);
-    rownorm_kernel<<<gf, 256, 0, stream>>>(P, R);
-    cudaError_t e = cudaGetLastError();
+cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, int2 *graze, float *glen, int *goff,
+                               int2 *graze_tmp, float *glen_tmp, int *gcnt, int capc, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(gcnt, 0, 4 * sizeof(int), stream);
     if (e != cudaSuccess) return e;
-    graze_list_kernel<<<1, 1024, 0, stream>>>(P, R, graze, glen, goff, capc);
+    dim3 gf((P.D + 31) / 32, (P.a + 7) / 8);
+    rownorm_kernel<<<gf, 256, 0, stream>>>(P, R, graze_tmp, glen_tmp, gcnt, capc);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    graze_sort_kernel<<<1, 1024, 0, stream>>>(graze_tmp, glen_tmp, gcnt, graze, glen, goff, capc);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     dim3 gb((P.N + 31) / 32, (P.N + 7) / 8);

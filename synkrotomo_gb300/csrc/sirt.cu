@@ -194,18 +194,16 @@ __device__ __forceinline__ double graze_ray(const SirtProblem &q, int s, int gid
 }
 
 // Backprojection terms of the listed rays that clip corner `corner` of slice
-// s, added in list order.
-__device__ __forceinline__ float corner_terms(const SirtProblem &q, int s, int corner) {
+// s, summed by the calling warp (lanes over the list, combined in a fixed
+// order); every lane returns the sum.
+__device__ __forceinline__ float corner_terms_warp(const SirtProblem &q, int s, int corner) {
+    const int lane = threadIdx.x & 31;
     const int n = __ldg(q.goff + corner + 1) - __ldg(q.goff + corner);
     const float *t = q.gcontrib + (size_t)s * 4 * q.graze_capc + (size_t)corner * q.graze_capc;
     float acc = 0.0f;
-    for (int i0 = 0; i0 < n; i0 += 8) {
-        float v[8];
+    for (int i = lane; i < n; i += 32) acc = __fadd_rn(acc, t[i]);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = i0 + j < n ? t[i0 + j] : 0.0f;   // loads in flight together
-#pragma unroll
-        for (int j = 0; j < 8; ++j) acc = __fadd_rn(acc, v[j]);             // acc + 0 is acc
-    }
+    for (int o = 16; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
     return acc;
 }
 
@@ -314,8 +312,8 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
             bp_stage(P, kc, sh.st);
             __syncthreads();
             float prt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            if (inrange) bp_chunk<4, true, true, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
-            else if (unit) bp_chunk<4, true, false, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            if (inrange) bp_chunk<4, true, true, true, 2>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+            else if (unit) bp_chunk<4, true, false, true, 2>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
             else bp_chunk<4, false, false, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
 #pragma unroll
             for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], prt[m]);
@@ -332,9 +330,19 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
                 float bpv = sh.red4[warp][m][lane];
                 for (int t = 1; t < SB; ++t) bpv += sh.red4[warp + t][m][lane];
                 const int row = row0 + RB * m;
-                // the image corners add the terms of the rays that clip only them
-                if ((row == 0 || row == P.N - 1) && (col == 0 || col == P.N - 1))
-                    bpv = __fadd_rn(bpv, corner_terms(q, s, (row == P.N - 1 ? 2 : 0) + (col == P.N - 1 ? 1 : 0)));
+                // the image corners add the terms of the rays that clip only
+                // them (the warp of a corner row sums them; warp-uniform tests)
+                if (row == 0 || row == P.N - 1) {
+                    const int cb = row == P.N - 1 ? 2 : 0;
+                    if (tx == 0) {
+                        const float t = corner_terms_warp(q, s, cb);
+                        if (col == 0) bpv = __fadd_rn(bpv, t);
+                    }
+                    if (tx == tx_n - 1) {
+                        const float t = corner_terms_warp(q, s, cb + 1);
+                        if (col == P.N - 1) bpv = __fadd_rn(bpv, t);
+                    }
+                }
                 float xi = 0.0f;
                 if (row < P.N && col < P.N) {
                     const size_t pix = (size_t)row * P.N + col;

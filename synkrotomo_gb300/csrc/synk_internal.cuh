@@ -339,10 +339,11 @@ cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float2 *xpai
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
                       float *scaled);
 // R, C and the lists of rays that only clip a corner pixel (their R stored
-// negated; graze [4*capc] entries {k, r} by corner, glen [4*capc] their
-// chords, goff [5] the prefix offsets; see rownorm_kernel / graze_list_kernel)
-cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, int2 *graze, float *glen, int *goff, int capc,
-                               cudaStream_t stream);
+// negated; graze [4*capc] entries {k, r} by corner in ray order, glen
+// [4*capc] their chords, goff [5] the prefix offsets; graze_tmp / glen_tmp
+// [4*capc] and gcnt [4] are scratch; see rownorm_kernel / graze_sort_kernel)
+cudaError_t launch_normalisers(const ProbGeom &P, float *R, float *C, int2 *graze, float *glen, int *goff,
+                               int2 *graze_tmp, float *glen_tmp, int *gcnt, int capc, cudaStream_t stream);
 
 // compare.cu: the validation programs (diff, mse, sanityCheck) in one pass.
 typedef synk_compare_result CompareResult;
