@@ -317,6 +317,19 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         if (q.iterations > 0) any_work = true;
         if (q.residuals) want_res = true;
     }
+    // Engine: one launch per phase and iteration (single problems, and small
+    // batches), the fused persistent kernel otherwise (grid_blocks == -1
+    // forces the split engine, > 0 the persistent kernel; 0 decides).
+    double work = 0.0;   // FP ray-row steps + BP (pixel, angle) pairs per iteration
+    for (int i = 0; i < nprob; ++i)
+        work += (double)in[i].nslices * (double)in[i].a * in[i].size * ((double)in[i].size + in[i].numrhos);
+    // (a captured plan keeps the persistent kernel unless forced: it cannot end the loop early)
+    const bool split = grid_blocks == -1 || (grid_blocks == 0 && !staging && (nprob == 1 || work <= kSmallWork));
+    int fpg = 0, bpg = 0;
+    if (split && !sirt_phase_grids(&fpg, &bpg)) return fail(ctx, SYNK_ECUDA, "SIRT phase kernels cannot be resident");
+    // the work splits fill the warps of the engine that runs the phases
+    const long long fp_warps = split ? (long long)fpg * 8 : resident_warps;
+    const long long bp_warps = split ? (long long)bpg * 8 : resident_warps;
     // start images
     for (int i = 0; i < nprob; ++i) {
         const synk_sirt_problem &q = in[i];
@@ -396,10 +409,11 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         // warp tasks per phase: one detector x 32 angles (FP), one 32-column x 4-row strip (BP)
         const long long fp_tasks = (long long)q.nslices * q.numrhos * ((q.a + 31) / 32);
         const long long bp_tasks = (long long)q.nslices * ((q.size + 3) / 4) * ((q.size + 31) / 32);
-        const long long share = nprob > 1 ? resident_warps / nprob + 1 : resident_warps;
+        const long long fp_share = nprob > 1 ? fp_warps / nprob + 1 : fp_warps;
+        const long long bp_share = nprob > 1 ? bp_warps / nprob + 1 : bp_warps;
         h.bp_inrange = bp_windows_in_range(h.P, 32) ? 1 : 0;   // BP tiles of 4*(8/bp_split) <= 32 rows
-        h.fp_split = q.fp_split ? q.fp_split : pick_fp_split(fp_tasks, share, q.size);
-        h.bp_split = q.bp_split ? q.bp_split : pick_bp_split(bp_tasks, share, q.a);
+        h.fp_split = q.fp_split ? q.fp_split : pick_fp_split(fp_tasks, fp_share, q.size);
+        h.bp_split = q.bp_split ? q.bp_split : pick_bp_split(bp_tasks, bp_share, q.a);
         h.fp_ips = h.bp_ips = 0;
         h.fp_begin = h.bp_begin = 0;
     }
@@ -445,17 +459,7 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
     sp.tol2 = tol > 0.0 ? tol * tol : 0.0;
     sp.record_final = want_res ? 1 : 0;
     sp.dynamic = nprob > 1 ? 1 : 0;
-    // Engine: one launch per phase and iteration (single problems, and small
-    // batches), the fused persistent kernel otherwise (grid_blocks == -1
-    // forces the split engine, > 0 the persistent kernel; 0 decides).
-    double work = 0.0;   // FP ray-row steps + BP (pixel, angle) pairs per iteration
-    for (int i = 0; i < nprob; ++i)
-        work += (double)in[i].nslices * (double)in[i].a * in[i].size * ((double)in[i].size + in[i].numrhos);
-    // (a captured plan keeps the persistent kernel unless forced: it cannot end the loop early)
-    const bool split = grid_blocks == -1 || (grid_blocks == 0 && !staging && (nprob == 1 || work <= kSmallWork));
     if (split) {
-        int fpg = 0, bpg = 0;
-        if (!sirt_phase_grids(&fpg, &bpg)) return fail(ctx, SYNK_ECUDA, "SIRT phase kernels cannot be resident");
         sp.dynamic = 0;
         int *active = reinterpret_cast<int *>(words + 7);
         // the early exit reads the active count on the host: not inside a graph

@@ -91,3 +91,33 @@ def test_spmv_csr32_caller_matrix(gpu):
     rc = ctx.lib.synk_spmv_csr32(ctx.handle, 300, rt._ptr(ptr), rt._ptr(idx), rt._ptr(val), rt._ptr(xd), rt._ptr(y))
     ctx.check(rc, "spmv")
     assert rel_l2(y.cpu().numpy(), M @ x.astype(np.float64)) < 1e-6
+
+
+def test_spmv_csr32_ragged_rows_and_nonfinite_x(gpu):
+    """Rows of 0..300 entries (partial 128-entry chunks at every offset) and a
+    non-finite x[0]: rows that do not hold column 0 stay finite and match the
+    float64 product, rows that do are +inf, empty rows are 0."""
+    rng = np.random.default_rng(1)
+    cols = 400
+    lens = [0, 1, 31, 32, 33, 96, 97, 127, 128, 129, 255, 256, 257, 300, 0, 5]
+    indptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    idx = np.concatenate([np.sort(rng.choice(np.arange(1, cols), n, replace=False)) for n in lens]).astype(np.int32)
+    idx[indptr[3]] = 0          # the row of 32 entries holds column 0
+    val = rng.random(idx.size).astype(np.float32) + 0.5
+    x = rng.random(cols).astype(np.float32)
+    x[0] = np.inf
+    rows = len(lens)
+    y = torch.full((rows,), -1.0, device="cuda")
+    ctx = rt.context()
+    args = [_dev(indptr), _dev(idx), _dev(val), _dev(x)]
+    rc = ctx.lib.synk_spmv_csr32(ctx.handle, rows, *[rt._ptr(t) for t in args], rt._ptr(y))
+    ctx.check(rc, "spmv")
+    got = y.cpu().numpy()
+    for r in range(rows):
+        sl = slice(indptr[r], indptr[r + 1])
+        if r == 3:
+            assert got[r] == np.inf
+            continue
+        ref = float(np.dot(val[sl].astype(np.float64), x[idx[sl]].astype(np.float64)))
+        assert np.isfinite(got[r]), r
+        assert abs(got[r] - ref) <= 1e-6 * max(abs(ref), 1.0), (r, got[r], ref)

@@ -116,11 +116,11 @@ def test_sirt3d_matches_reference_semantics(gpu):
 
 
 def test_phase_split_engine_matches_persistent(gpu):
-    """grid_blocks=-1 runs one launch per phase and iteration.  The same items
-    compute the same values, so without a stopping rule the iterates are
-    bit-identical to the persistent kernel's; with one, every slice stops at
-    the same iteration (the loop then ends on the host's check of the active
-    count after iteration 16, 32, ...)."""
+    """grid_blocks=-1 runs one launch per phase and iteration.  With the same
+    work splits the same items compute the same values, so without a stopping
+    rule the iterates are bit-identical to the persistent kernel's; with one,
+    every slice stops at the same iteration (the loop then ends on the host's
+    check of the active count after iteration 16, 32, ...)."""
     size, a, ns, its = 48, 40, 6, 45
     g = phantom.geometry(size, a)
     vol = phantom.ellipsoid_volume(size, ns, seed=3)
@@ -128,10 +128,11 @@ def test_phase_split_engine_matches_persistent(gpu):
                       for i in range(ns)])
     ang, bd = _dev(g.angles), _dev(sinos.ravel())
     full = rt.resident_blocks()
+    kw = dict(fp_split=2, bp_split=4)
     xp, rp, dp = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
-                                grid_blocks=full)
+                                grid_blocks=full, **kw)
     xs, rs, ds = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
-                                grid_blocks=-1)
+                                grid_blocks=-1, **kw)
     assert torch.equal(xp, xs)
     assert torch.equal(dp, ds)
     np.testing.assert_allclose(rs.cpu().numpy(), rp.cpu().numpy(), rtol=1e-12)
@@ -141,9 +142,9 @@ def test_phase_split_engine_matches_persistent(gpu):
     hist = rp.cpu().numpy()
     tol = float(np.median(hist[:, 20]))
     xp2, _, dp2 = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, tol=tol,
-                                 grid_blocks=full)
+                                 grid_blocks=full, **kw)
     xs2, _, ds2 = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, tol=tol,
-                                 grid_blocks=-1)
+                                 grid_blocks=-1, **kw)
     assert torch.equal(dp2, ds2)
     assert torch.equal(xp2, xs2)
     assert int(ds2.min()) < its and int(ds2.max()) > 16
@@ -166,8 +167,10 @@ def test_phase_split_engine_uneven_batch(gpu):
 
 def test_phase_split_engine_large_stack_matches_persistent(gpu):
     """Above 6e7 work per iteration a single problem's forward phase runs on the
-    projector's grid (sirt_fp_stack_kernel): the same per-ray values, so the
-    iterates equal the persistent kernel's bit for bit."""
+    projector's grid (sirt_fp_stack_kernel): with the same work splits the
+    per-ray values are the same, so the iterates equal the persistent kernel's
+    bit for bit.  With the splits each engine picks for its own grid the sums
+    run in another order and the iterates agree to rounding."""
     size, a, ns, its = 256, 180, 4, 12
     g = phantom.geometry(size, a)
     vol = phantom.ellipsoid_volume(size, ns, seed=5)
@@ -175,11 +178,17 @@ def test_phase_split_engine_large_stack_matches_persistent(gpu):
                       for i in range(ns)])
     ang, bd = _dev(g.angles), _dev(sinos.ravel())
     assert ns * a * size * (size + g.numrhos) > 6e7
-    xp, rp, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
-                               grid_blocks=rt.resident_blocks())
+    for fs, bs in ((2, 4), (8, 1)):
+        xp, rp, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
+                                   fp_split=fs, bp_split=bs, grid_blocks=rt.resident_blocks())
+        xs, rs, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
+                                   fp_split=fs, bp_split=bs, grid_blocks=-1)
+        assert torch.equal(xp, xs), (fs, bs)
+        np.testing.assert_allclose(rs.cpu().numpy(), rp.cpu().numpy(), rtol=1e-12)
+    xp, _, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its,
+                              grid_blocks=rt.resident_blocks())
     xs, rs, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
                                grid_blocks=-1)
-    assert torch.equal(xp, xs)
-    np.testing.assert_allclose(rs.cpu().numpy(), rp.cpu().numpy(), rtol=1e-12)
+    assert rel_l2(xs.cpu().numpy(), xp.cpu().numpy()) < 1e-6
     ref = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), sinos[1], its)
     assert rel_l2(xs.cpu().numpy().reshape(ns, -1)[1], ref) < 1e-5
