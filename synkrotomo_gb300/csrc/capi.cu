@@ -327,6 +327,9 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
     const bool split = grid_blocks == -1 || (grid_blocks == 0 && !staging && (nprob == 1 || work <= kSmallWork));
     int fpg = 0, bpg = 0;
     if (split && !sirt_phase_grids(&fpg, &bpg)) return fail(ctx, SYNK_ECUDA, "SIRT phase kernels cannot be resident");
+    // one large problem: the split engine's forward phase on the projector's own grid
+    const bool stack = split && nprob == 1 && work > kSmallWork && in[0].nslices <= 65535 &&
+                       (in[0].a + 31) / 32 + 2 <= 65535;
     // the work splits fill the warps of the engine that runs the phases
     const long long fp_warps = split ? (long long)fpg * 8 : resident_warps;
     const long long bp_warps = split ? (long long)bpg * 8 : resident_warps;
@@ -414,6 +417,28 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         h.bp_inrange = bp_windows_in_range(h.P, 32) ? 1 : 0;   // BP tiles of 4*(8/bp_split) <= 32 rows
         h.fp_split = q.fp_split ? q.fp_split : pick_fp_split(fp_tasks, fp_share, q.size);
         h.bp_split = q.bp_split ? q.bp_split : pick_bp_split(bp_tasks, bp_share, q.a);
+        // The phase kernels' items are blocks of 8 warps.  Measured with the
+        // split engine at N=64/128/256 (1 slice, 200 iterations), its forward
+        // phase is fastest with the rays' rows split as far as keeps the warps
+        // at about 3/4 of the resident ones (S = 8/4/2 there, parts of >= 8
+        // rows): N=128 5.88 -> 4.69 ms together with the backward phase's
+        // fewest pixels per thread (1 of 4) that still give 3/4 of the
+        // resident blocks an item (4.25 -> 3.44 ms at N=64).
+        if (split && !stack && !q.fp_split) {
+            const int maxs = q.size / 8 > 8 ? 8 : (q.size / 8 < 1 ? 1 : q.size / 8);
+            int S = 1;
+            while (S < maxs && fp_tasks * S * 2 * 4 <= fp_share * 3) S *= 2;
+            h.fp_split = S;
+        }
+        h.bp_pix = 4;
+        const long long tiles_x = (q.size + 31) / 32;
+        const long long bp_blocks = (split ? bpg : grid) / (nprob > 1 ? nprob : 1) + 1;
+        while (h.bp_pix > 1) {
+            const int TR = h.bp_pix * (8 / h.bp_split);
+            const long long items = (long long)q.nslices * tiles_x * ((q.size + TR - 1) / TR);
+            if (items * 4 >= bp_blocks * 3) break;
+            h.bp_pix >>= 1;
+        }
         h.fp_ips = h.bp_ips = 0;
         h.fp_begin = h.bp_begin = 0;
     }
@@ -467,9 +492,6 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusNone;
         const bool can_poll = sp.tol2 > 0.0 && !staging && cap == cudaStreamCaptureStatusNone;
-        // one large problem: the forward phase on the projector's own grid
-        const bool stack = nprob == 1 && work > kSmallWork && host[0].nslices <= 65535 &&
-                           (host[0].P.a + 31) / 32 + 2 <= 65535;
         for (int it = 0; it <= max_iter; ++it) {
             if (stack) SYNK_CUDA(launch_sirt_fp_stack(host[0], it, sp.tol2, sp.record_final, st), "SIRT forward phase");
             else SYNK_CUDA(launch_sirt_fp_phase(sp, it, fpg, st), "SIRT forward phase");

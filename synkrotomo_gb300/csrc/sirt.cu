@@ -281,85 +281,102 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
 }
 
 // ---- phase BP of iteration `it` ------------------------------------------------
-__device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtShared &sh) {
+// One item: a tile of 32 columns x PIX*(8/bp_split) rows of slice s; thread
+// (lane, warp) sums PIX rows of one column over its part of the angles.
+template <int PIX>
+__device__ __forceinline__ void bp_item(const SirtProblem &q, int s, int rem, SirtShared &sh) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ProbGeom &P = q.P;
+    const int SB = q.bp_split, RB = 8 / SB;          // angle parts, warp rows
+    const int TR = PIX * RB;                         // tile rows
+    const int tx_n = (P.N + 31) / 32;
+    const int ty = rem / tx_n;
+    const int tx = rem - ty * tx_n;
+    const int wrow = warp / SB, part = warp % SB;
+    const size_t pr = (size_t)P.a * P.D, np = (size_t)P.N * (P.N + 2);
+    const int col = tx * 32 + lane;
+    const int row0 = ty * TR + wrow;
+    const float xc = (float)(col - P.half) + 0.5f;
+    const float yc0 = (float)(row0 - P.half) + 0.5f;
+    const float *rr = q.rr + (size_t)s * pr;
+    const bool unit = P.deltarho == 1.0f;
+    const bool inrange = q.bp_inrange != 0;
+    float sum[PIX], comp[PIX];
+#pragma unroll
+    for (int m = 0; m < PIX; ++m) sum[m] = comp[m] = 0.0f;
+    for (int kc = 0; kc < P.a; kc += kBpChunk) {
+        __syncthreads();
+        bp_stage(P, kc, sh.st);
+        __syncthreads();
+        float prt[PIX];
+#pragma unroll
+        for (int m = 0; m < PIX; ++m) prt[m] = 0.0f;
+        if (inrange) bp_chunk<PIX, true, true, true, 2>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+        else if (unit) bp_chunk<PIX, true, false, true, 2>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+        else bp_chunk<PIX, false, false, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
+#pragma unroll
+        for (int m = 0; m < PIX; ++m) comp_add(sum[m], comp[m], prt[m]);
+    }
+    float ex[PIX];
+#pragma unroll
+    for (int m = 0; m < PIX; ++m) ex[m] = 0.0f;
+    bp_exact_angles<PIX>(P, q.L.exact, __ldg(q.L.counts + 2), part, SB, rr, row0, RB, col, ex);
+#pragma unroll
+    for (int m = 0; m < PIX; ++m) sh.red4[warp][m][lane] = (sum[m] + comp[m]) + ex[m];
+    __syncthreads();
+    float *xpad = q.xpad + (size_t)s * np;
+    if (part == 0) {
+#pragma unroll
+        for (int m = 0; m < PIX; ++m) {
+            float bpv = sh.red4[warp][m][lane];
+            for (int t = 1; t < SB; ++t) bpv += sh.red4[warp + t][m][lane];
+            const int row = row0 + RB * m;
+            // the image corners add the terms of the rays that clip only
+            // them (the warp of a corner row sums them; warp-uniform tests)
+            if (row == 0 || row == P.N - 1) {
+                const int cb = row == P.N - 1 ? 2 : 0;
+                if (tx == 0) {
+                    const float t = corner_terms_warp(q, s, cb);
+                    if (col == 0) bpv = __fadd_rn(bpv, t);
+                }
+                if (tx == tx_n - 1) {
+                    const float t = corner_terms_warp(q, s, cb + 1);
+                    if (col == P.N - 1) bpv = __fadd_rn(bpv, t);
+                }
+            }
+            float xi = 0.0f;
+            if (row < P.N && col < P.N) {
+                const size_t pix = (size_t)row * P.N + col;
+                float *xp = xpad + (size_t)row * (P.N + 2) + col + 1;
+                xi = __fadd_rn(*xp, __fmul_rn(q.C[pix], bpv));             // SIRT.fut:38-39
+                *xp = xi;
+            }
+            sh.tile[lane][wrow + RB * m] = xi;
+        }
+    }
+    __syncthreads();
+    // transposed write: xTpad[col][row + 1] for the tile's 32 columns x TR rows
+    float *xTpad = q.xTpad + (size_t)s * np;
+    for (int i = threadIdx.x; i < 32 * TR; i += blockDim.x) {
+        const int cl = i / TR, rl = i - cl * TR;
+        const int c = tx * 32 + cl, r = ty * TR + rl;
+        if (c < P.N && r < P.N) xTpad[(size_t)c * (P.N + 2) + r + 1] = sh.tile[cl][rl];
+    }
+}
+
+__device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtShared &sh) {
     const long long total = p.totals[1];
     for (long long item = next_item(p, counter, -1, sh); item < total; item = next_item(p, counter, item, sh)) {
         const int qi = find_problem(p, item, false);
         const SirtProblem &q = p.probs[qi];
-        const ProbGeom &P = q.P;
         const long long local = item - q.bp_begin;
         const int s = (int)(local / q.bp_ips);
         const int rem = (int)(local - (long long)s * q.bp_ips);
         if (!bp_needed(p, q, s, it)) continue;            // uniform over the block
-        const int SB = q.bp_split, RB = 8 / SB;          // angle parts, warp rows
-        const int TR = 4 * RB;                           // tile rows
-        const int tx_n = (P.N + 31) / 32;
-        const int ty = rem / tx_n;
-        const int tx = rem - ty * tx_n;
-        const int wrow = warp / SB, part = warp % SB;
-        const size_t pr = (size_t)P.a * P.D, np = (size_t)P.N * (P.N + 2);
-        const int col = tx * 32 + lane;
-        const int row0 = ty * TR + wrow;
-        const float xc = (float)(col - P.half) + 0.5f;
-        const float yc0 = (float)(row0 - P.half) + 0.5f;
-        const float *rr = q.rr + (size_t)s * pr;
-        const bool unit = P.deltarho == 1.0f;
-        const bool inrange = q.bp_inrange != 0;
-        float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f}, comp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int kc = 0; kc < P.a; kc += kBpChunk) {
-            __syncthreads();
-            bp_stage(P, kc, sh.st);
-            __syncthreads();
-            float prt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            if (inrange) bp_chunk<4, true, true, true, 2>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
-            else if (unit) bp_chunk<4, true, false, true, 2>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
-            else bp_chunk<4, false, false, true>(P, sh.st, kc, P.a, part, SB, rr, xc, yc0, (float)RB, prt);
-#pragma unroll
-            for (int m = 0; m < 4; ++m) comp_add(sum[m], comp[m], prt[m]);
-        }
-        float ex[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        bp_exact_angles<4>(P, q.L.exact, __ldg(q.L.counts + 2), part, SB, rr, row0, RB, col, ex);
-#pragma unroll
-        for (int m = 0; m < 4; ++m) sh.red4[warp][m][lane] = (sum[m] + comp[m]) + ex[m];
-        __syncthreads();
-        float *xpad = q.xpad + (size_t)s * np;
-        if (part == 0) {
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                float bpv = sh.red4[warp][m][lane];
-                for (int t = 1; t < SB; ++t) bpv += sh.red4[warp + t][m][lane];
-                const int row = row0 + RB * m;
-                // the image corners add the terms of the rays that clip only
-                // them (the warp of a corner row sums them; warp-uniform tests)
-                if (row == 0 || row == P.N - 1) {
-                    const int cb = row == P.N - 1 ? 2 : 0;
-                    if (tx == 0) {
-                        const float t = corner_terms_warp(q, s, cb);
-                        if (col == 0) bpv = __fadd_rn(bpv, t);
-                    }
-                    if (tx == tx_n - 1) {
-                        const float t = corner_terms_warp(q, s, cb + 1);
-                        if (col == P.N - 1) bpv = __fadd_rn(bpv, t);
-                    }
-                }
-                float xi = 0.0f;
-                if (row < P.N && col < P.N) {
-                    const size_t pix = (size_t)row * P.N + col;
-                    float *xp = xpad + (size_t)row * (P.N + 2) + col + 1;
-                    xi = __fadd_rn(*xp, __fmul_rn(q.C[pix], bpv));             // SIRT.fut:38-39
-                    *xp = xi;
-                }
-                sh.tile[lane][wrow + RB * m] = xi;
-            }
-        }
-        __syncthreads();
-        // transposed write: xTpad[col][row + 1] for the tile's 32 columns x TR rows
-        float *xTpad = q.xTpad + (size_t)s * np;
-        for (int i = threadIdx.x; i < 32 * TR; i += blockDim.x) {
-            const int cl = i / TR, rl = i - cl * TR;
-            const int c = tx * 32 + cl, r = ty * TR + rl;
-            if (c < P.N && r < P.N) xTpad[(size_t)c * (P.N + 2) + r + 1] = sh.tile[cl][rl];
+        switch (q.bp_pix) {                               // uniform over the block
+            case 1: bp_item<1>(q, s, rem, sh); break;
+            case 2: bp_item<2>(q, s, rem, sh); break;
+            default: bp_item<4>(q, s, rem, sh); break;
         }
     }
 }
@@ -513,7 +530,7 @@ __global__ void sirt_plan_kernel(SirtProblem *probs, int nprob, long long *total
         const int ngroups = q.L.counts[0] + q.L.counts[1];
         const int nexact = q.L.counts[2];
         q.fp_ips = ngroups * ((q.P.D + G - 1) / G) + nexact * ((q.P.D + 7) / 8) + (q.goff[4] + 7) / 8;
-        const int TR = 4 * (8 / q.bp_split);
+        const int TR = q.bp_pix * (8 / q.bp_split);
         q.bp_ips = ((q.P.N + 31) / 32) * ((q.P.N + TR - 1) / TR);
         q.fp_begin = fb;
         q.bp_begin = bb;

@@ -29,6 +29,7 @@ struct SirtProblem {
     int iterations;
     int fp_split;         // 1,2,4,8 warps share one ray (rows split)
     int bp_split;         // 1,2,4,8 warps share one pixel (angles split)
+    int bp_pix;           // 1,2,4 pixels (rows) per thread in the backward phase
     int bp_inrange;       // every pixel's detector window is inside the sinogram (no bounds checks)
     int graze_capc;       // capacity of one corner's list
     // filled on the device by sirt_plan_kernel (they depend on the angle lists)
