@@ -95,7 +95,7 @@ struct SirtShared {
     float red[8][33];
     float red4[8][4][32];
     float tile[32][33];
-    double e2;
+    double e2w[8];        // per-warp e^2 partials of a flush
     long long item;
     int flag;
     int any;
@@ -207,11 +207,41 @@ __device__ __forceinline__ float corner_terms_warp(const SirtProblem &q, int s, 
     return acc;
 }
 
-__device__ __forceinline__ void flush_e2(int it, const SirtProblem *q, int slice, SirtShared &sh) {
-    if (threadIdx.x == 0 && q) {
-        atomicAdd(q->res2 + (size_t)slice * (q->iterations + 1) + it, sh.e2);
-        sh.e2 = 0.0;
+// Adds the block's e^2 of (problem q, slice) to its residual sum: every lane
+// holds a partial; the warps' sums are added in warp order.  Called by the
+// whole block at block-uniform points (q and slice are uniform).
+__device__ __forceinline__ void flush_e2(int it, const SirtProblem *q, int slice, double &acc, SirtShared &sh) {
+    if (!q) return;
+    const double w = warp_sum_d(acc);
+    acc = 0.0;
+    if ((threadIdx.x & 31) == 0) sh.e2w[threadIdx.x >> 5] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh.e2w[i];
+        if (t != 0.0) atomicAdd(q->res2 + (size_t)slice * (q->iterations + 1) + it, t);
     }
+    // e2w is written again only after the next block-wide barrier
+}
+
+// Slice and item-in-slice of a problem-local item (32-bit division when the
+// index fits).
+__device__ __forceinline__ void item_slice(long long local, int ips, int &s, int &rem) {
+    if (local <= 0x7fffffffLL) {
+        const unsigned l = (unsigned)local, u = (unsigned)ips;
+        s = (int)(l / u);
+        rem = (int)(l - (unsigned)s * u);
+    } else {
+        s = (int)(local / ips);
+        rem = (int)(local - (long long)s * ips);
+    }
+}
+
+// Rows [jb, je) of part `part` of S (a power of two) equal parts of N rows.
+__device__ __forceinline__ void row_part(int N, int S, int part, int &jb, int &je) {
+    const int sh = __ffs(S) - 1;
+    jb = (part * N) >> sh;
+    je = ((part + 1) * N) >> sh;
 }
 
 // ---- phase FP of iteration `it` ------------------------------------------------
@@ -220,34 +250,34 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
     const long long total = p.totals[0];
     const SirtProblem *cur = nullptr;
     int cur_slice = -1;
-    if (threadIdx.x == 0) sh.e2 = 0.0;
+    double e2acc = 0.0;                                   // this lane's e^2 of (cur, cur_slice)
     for (long long item = next_item(p, counter, -1, sh); item < total; item = next_item(p, counter, item, sh)) {
         const int qi = find_problem(p, item, true);
         const SirtProblem &q = p.probs[qi];
         const ProbGeom &P = q.P;
-        const long long local = item - q.fp_begin;
-        const int s = (int)(local / q.fp_ips);
-        const int rem = (int)(local - (long long)s * q.fp_ips);
-        __syncthreads();                                  // red / e2 reuse
+        int s, rem;
+        item_slice(item - q.fp_begin, q.fp_ips, s, rem);
+        __syncthreads();                                  // red reuse
         if (&q != cur || s != cur_slice) {
-            flush_e2(it, cur, cur_slice, sh);
+            flush_e2(it, cur, cur_slice, e2acc, sh);
             cur = &q;
             cur_slice = s;
         }
         if (!fp_needed(p, q, s, it)) continue;            // uniform over the block
-        const int S = q.fp_split, G = 8 / S;
+        const int S = q.fp_split, lgS = __ffs(S) - 1, G = 8 >> lgS;
         const int ngroups = __ldg(q.L.counts) + __ldg(q.L.counts + 1);
         const int nsteep = __ldg(q.L.counts);
-        const int dblocks = (P.D + G - 1) / G;
+        const int dblocks = (P.D + G - 1) >> (3 - lgS);
         const int fast_items = ngroups * dblocks;
         const size_t np = (size_t)P.N * (P.N + 2);
         double e2 = 0.0;
         if (rem < fast_items) {
-            const int part = warp % S;
-            const int jb = (int)((long long)part * P.N / S), je = (int)((long long)(part + 1) * P.N / S);
-            const int grp = rem / dblocks;
+            const int part = warp & (S - 1);
+            int jb, je;
+            row_part(P.N, S, part, jb, je);
+            const int grp = (int)((unsigned)rem / (unsigned)dblocks);
             const int db = rem - grp * dblocks;
-            const int r = db * G + warp / S;
+            const int r = db * G + (warp >> lgS);
             const int k = r < P.D ? __ldg(q.L.order + grp * 32 + lane) : -1;
             const float *img = (grp < nsteep ? q.xpad : q.xTpad) + (size_t)s * np;
             const float v = fp_lane_ray(P, k, r, img, jb, je);
@@ -273,11 +303,10 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
             const int gidx = (rem - fast_items - __ldg(q.L.counts + 2) * ((P.D + 7) / 8)) * 8 + warp;
             if (gidx < graze_count(q)) e2 = graze_ray(q, s, gidx);      // warp-uniform
         }
-        e2 = warp_sum_d(e2);
-        if (lane == 0) atomicAdd(&sh.e2, e2);
+        e2acc += e2;
     }
     __syncthreads();
-    flush_e2(it, cur, cur_slice, sh);
+    flush_e2(it, cur, cur_slice, e2acc, sh);
 }
 
 // ---- phase BP of iteration `it` ------------------------------------------------
@@ -287,12 +316,12 @@ template <int PIX>
 __device__ __forceinline__ void bp_item(const SirtProblem &q, int s, int rem, SirtShared &sh) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const ProbGeom &P = q.P;
-    const int SB = q.bp_split, RB = 8 / SB;          // angle parts, warp rows
+    const int SB = q.bp_split, lgSB = __ffs(SB) - 1, RB = 8 >> lgSB;   // angle parts, warp rows
     const int TR = PIX * RB;                         // tile rows
-    const int tx_n = (P.N + 31) / 32;
-    const int ty = rem / tx_n;
+    const int tx_n = (P.N + 31) >> 5;
+    const int ty = (int)((unsigned)rem / (unsigned)tx_n);
     const int tx = rem - ty * tx_n;
-    const int wrow = warp / SB, part = warp % SB;
+    const int wrow = warp >> lgSB, part = warp & (SB - 1);
     const size_t pr = (size_t)P.a * P.D, np = (size_t)P.N * (P.N + 2);
     const int col = tx * 32 + lane;
     const int row0 = ty * TR + wrow;
@@ -369,9 +398,8 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
     for (long long item = next_item(p, counter, -1, sh); item < total; item = next_item(p, counter, item, sh)) {
         const int qi = find_problem(p, item, false);
         const SirtProblem &q = p.probs[qi];
-        const long long local = item - q.bp_begin;
-        const int s = (int)(local / q.bp_ips);
-        const int rem = (int)(local - (long long)s * q.bp_ips);
+        int s, rem;
+        item_slice(item - q.bp_begin, q.bp_ips, s, rem);
         if (!bp_needed(p, q, s, it)) continue;            // uniform over the block
         switch (q.bp_pix) {                               // uniform over the block
             case 1: bp_item<1>(q, s, rem, sh); break;
