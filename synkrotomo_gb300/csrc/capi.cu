@@ -420,14 +420,14 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         // The phase kernels' items are blocks of 8 warps.  Measured with the
         // split engine at N=64/128/256 (1 slice, 200 iterations), its forward
         // phase is fastest with the rays' rows split as far as keeps the warps
-        // at about 3/4 of the resident ones (S = 8/4/2 there, parts of >= 8
-        // rows): N=128 5.88 -> 4.69 ms together with the backward phase's
-        // fewest pixels per thread (1 of 4) that still give 3/4 of the
-        // resident blocks an item (4.25 -> 3.44 ms at N=64).
+        // within the resident ones (S = 8/8/2 there, parts of >= 8 rows), and
+        // the backward phase with the fewest pixels per thread (1 of 4) that
+        // still give 3/4 of the resident blocks an item: N=128 5.88 -> 4.69 ms,
+        // N=64 4.25 -> 3.44 ms (before the chained launches).
         if (split && !stack && !q.fp_split) {
             const int maxs = q.size / 8 > 8 ? 8 : (q.size / 8 < 1 ? 1 : q.size / 8);
             int S = 1;
-            while (S < maxs && fp_tasks * S * 2 * 4 <= fp_share * 3) S *= 2;
+            while (S < maxs && fp_tasks * S * 2 <= fp_share) S *= 2;
             h.fp_split = S;
         }
         h.bp_pix = 4;

@@ -440,6 +440,16 @@ __global__ void __launch_bounds__(256, 3) sirt_persistent_kernel(SirtParams p) {
     }
 }
 
+// Programmatic dependent launch: a phase kernel launched with programmatic
+// stream serialization lets the next one be scheduled once all of its blocks
+// have started (launch_dependents), and the next one's blocks wait in
+// griddepcontrol.wait until this grid has completed and its writes are
+// visible.  Every block waits before it reads anything an earlier kernel
+// wrote, and before it exits, so completion stays transitive along the chain.
+// Launched without the attribute both instructions return at once.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Phase-split engine: the same two phases as ordinary launches, one per phase
 // and iteration.  The kernel boundary replaces the grid barrier, which for
 // small iterations (a few slices of N <= 256) is cheaper than the persistent
@@ -447,6 +457,8 @@ __global__ void __launch_bounds__(256, 3) sirt_persistent_kernel(SirtParams p) {
 // allocation.  Items are assigned statically (item = block + i*grid).
 __global__ void __launch_bounds__(256, 5) sirt_fp_phase_kernel(SirtParams p, int it) {
     __shared__ SirtShared sh;
+    chain_release();
+    chain_wait();
     fp_phase(p, it, nullptr, sh);
 }
 
@@ -530,6 +542,8 @@ __global__ void __launch_bounds__(256) sirt_fp_stack_exact_kernel(SirtProblem q,
 // stores the number of slices still updating in *active.
 __global__ void __launch_bounds__(256, 4) sirt_bp_phase_kernel(SirtParams p, int it, int *active) {
     __shared__ SirtShared sh;
+    chain_release();
+    chain_wait();
     if (blockIdx.x == 0) {
         if (threadIdx.x == 0) sh.any = 0;
         __syncthreads();
@@ -643,9 +657,25 @@ int sirt_phase_grids(int *fp_grid, int *bp_grid) {
     return f > 0 && b > 0;
 }
 
+// A launch of 256-thread blocks that may begin while the previous kernel in
+// the stream finishes (programmatic stream serialization; the kernel waits).
+template <class... KArgs, class... Args>
+static cudaError_t launch_chained(void (*kernel)(KArgs...), int grid, cudaStream_t stream, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 cudaError_t launch_sirt_fp_phase(const SirtParams &p, int it, int grid, cudaStream_t stream) {
-    sirt_fp_phase_kernel<<<grid, 256, 0, stream>>>(p, it);
-    return cudaGetLastError();
+    return launch_chained(sirt_fp_phase_kernel, grid, stream, p, it);
 }
 
 cudaError_t launch_sirt_fp_stack(const SirtProblem &q, int it, double tol2, int record_final, cudaStream_t stream) {
@@ -666,8 +696,7 @@ cudaError_t launch_sirt_fp_stack(const SirtProblem &q, int it, double tol2, int 
 }
 
 cudaError_t launch_sirt_bp_phase(const SirtParams &p, int it, int *active, int grid, cudaStream_t stream) {
-    sirt_bp_phase_kernel<<<grid, 256, 0, stream>>>(p, it, active);
-    return cudaGetLastError();
+    return launch_chained(sirt_bp_phase_kernel, grid, stream, p, it, active);
 }
 
 cudaError_t launch_sirt_persistent(const SirtParams &p, int grid, cudaStream_t stream) {
