@@ -62,10 +62,13 @@ __device__ __forceinline__ void bp_stage(const ProbGeom &P, int k0, BpStage &st)
 // (pixel, angle); near-axis rows stay unscaled for bp_exact_angles.
 // UNR = 2 walks the angles in pairs, so that both angles' gathers are in flight
 // together; the sums stay in angle order, bit for bit those of UNR = 1.
+// PAIR (INRANGE only): sino holds detector pairs, entry s of row k =
+// (row[s], row[s+1]) at float offset 2*(k*D + s), so one 8-byte gather serves
+// both candidates (the same values, the same sums).
 // Measured on GB300: SIRT at N=128 6.20 -> 5.88 ms (200 iterations; few warps
 // there hide the gathers' latency), the dense backprojector at N=2048 4.88 ->
 // 4.73 ms.
-template <int PIX, bool UNIT, bool INRANGE, bool SCALED, int UNR = 1>
+template <int PIX, bool UNIT, bool INRANGE, bool SCALED, int UNR = 1, bool PAIR = false>
 __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, int kc, int kend, int kphase,
                                          int kstride, const float *__restrict__ sino, float xc, float yc0,
                                          float ystep, float (&acc)[PIX]) {
@@ -75,11 +78,12 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
     const int nk = min(kBpChunk, kend - kc);
     const float zoff = -P.rz_c - fact;        // centred: |q| stays below ~N/sqrt(2) + 1
     // INRANGE gather base: row + zi - kMagicBits (the magic constant's bits folded in)
-    const uintptr_t zoffb = (uintptr_t)(((intptr_t)P.zi - (intptr_t)kMagicBits) * 4);
+    static_assert(!PAIR || INRANGE, "pair rows only on the in-range path");
+    const uintptr_t zoffb = (uintptr_t)(((intptr_t)P.zi - (intptr_t)kMagicBits) * (PAIR ? 8 : 4));
     auto angle = [&](int i) {
         const float4 g = st.cs[i];
         const float2 le = st.le[i];
-        const float *__restrict__ row = sino + (size_t)(kc + i) * D;
+        const float *__restrict__ row = sino + (size_t)(kc + i) * D * (PAIR ? 2 : 1);
         if constexpr (UNIT) {
             // q of pixel m from the angle's base value in one rounding
             // (fma(m, dq, q0)), not by repeated additions: those drift by up
@@ -98,10 +102,17 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
                 if constexpr (INRANGE) {
                     const float r = __fadd_ru(q, kMagic);
                     e = __fsub_rn(r, kMagic) - q;
-                    const float *p = reinterpret_cast<const float *>(
-                        rowb + (uintptr_t)(unsigned)__float_as_int(r) * 4u);
-                    v0 = __ldg(p);
-                    v1 = __ldg(p + 1);
+                    if constexpr (PAIR) {
+                        const float2 v = __ldg(reinterpret_cast<const float2 *>(
+                            rowb + (uintptr_t)(unsigned)__float_as_int(r) * 8u));
+                        v0 = v.x;
+                        v1 = v.y;
+                    } else {
+                        const float *p = reinterpret_cast<const float *>(
+                            rowb + (uintptr_t)(unsigned)__float_as_int(r) * 4u);
+                        v0 = __ldg(p);
+                        v1 = __ldg(p + 1);
+                    }
                 } else {
                     int s0;
                     e = ceil_magic(q, s0) - q;

@@ -242,15 +242,15 @@ int backward(synk_context *ctx, float *out, const float *angles, int64_t a, floa
     cudaStream_t st = ctx->stream;
     Scratch sc(st);
     AngleGeom *geom;
-    SYNK_CUDA(sc.reserve(Scratch::round(sizeof(AngleGeom) * (size_t)a) + Scratch::round(sizeof(float) * (size_t)p) +
-                         lists_bytes(a)),
+    SYNK_CUDA(sc.reserve(Scratch::round(sizeof(AngleGeom) * (size_t)a) +
+                         Scratch::round(sizeof(float) * 2 * (size_t)p) + lists_bytes(a)),
               "cudaMallocAsync(scratch)");
     SYNK_CUDA(sc.get(&geom, (size_t)a), "cudaMallocAsync(geometry)");
     const ProbGeom P = make_geom(a, rhozero, deltarho, numrhos, size_in, geom);
     AngleLists L;
     SYNK_CUDA(make_setup(sc, angles, P, &L, st), "setup kernel");
-    float *scaled;
-    SYNK_CUDA(sc.get(&scaled, (size_t)p), "cudaMallocAsync(scaled rows)");
+    float *scaled;   // scaled rows, or scaled detector pairs (launch_bp)
+    SYNK_CUDA(sc.get(&scaled, 2 * (size_t)p), "cudaMallocAsync(scaled rows)");
     SYNK_CUDA(launch_bp(P, L, projections, out, st, scaled), "backprojection kernel");
     return SYNK_OK;
 }

@@ -483,6 +483,19 @@ __global__ void __launch_bounds__(256) row_scale_kernel(ProbGeom P, const float 
     sino_s[i] = sino[i] * row_scale(P.geom, k);
 }
 
+// pair[k][s] = (v[s], v[s+1]) with v = sino[k] * row_scale(k) and v[D] = 0:
+// the rows of a SCALED backprojection as detector pairs (bp_chunk's PAIR).
+__global__ void __launch_bounds__(256) row_pair_kernel(ProbGeom P, const float *__restrict__ sino,
+                                                       float2 *__restrict__ pair) {
+    const int r = blockIdx.x * 256 + threadIdx.x;
+    const int k = blockIdx.y;
+    if (r >= P.D) return;
+    const size_t i = (size_t)k * P.D + r;
+    const float sc = row_scale(P.geom, k);
+    const float v1 = r + 1 < P.D ? sino[i + 1] * sc : 0.0f;
+    pair[i] = make_float2(sino[i] * sc, v1);
+}
+
 // Pixels per thread of the standalone backprojector (rows 8 apart: a block
 // covers 32 columns x 8*PIX rows), and the resident blocks per SM each variant
 // is compiled for.  8 pixels halve the per-angle overhead (dense data: 4.80 ms
@@ -496,7 +509,7 @@ constexpr int kBpManyAngles = 256;     // angle count from which the 8-pixel var
 
 // sino_s: the fast-path rows (scaled when SCALED, else sino itself); sino:
 // the unscaled rows read by the near-axis angles.
-template <int kBpPix, bool UNIT, bool INRANGE, bool SCALED>
+template <int kBpPix, bool UNIT, bool INRANGE, bool SCALED, bool PAIR = false>
 __global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_tile_kernel(ProbGeom P, AngleLists L,
                                                                    const float *__restrict__ sino_s,
                                                                    const float *__restrict__ sino,
@@ -517,7 +530,7 @@ __global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_tile_kern
         float part[kBpPix];
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) part[m] = 0.0f;
-        bp_chunk<kBpPix, UNIT, INRANGE, SCALED, 2>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
+        bp_chunk<kBpPix, UNIT, INRANGE, SCALED, 2, PAIR>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) comp_add(sum[m], comp[m], part[m]);
     }
@@ -615,7 +628,12 @@ static void launch_bp_pix(const ProbGeom &P, const AngleLists &L, const float *s
 
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
                       float *scaled) {
-    if (scaled) {
+    if (scaled && P.a >= kBpManyAngles && bp_angle_split(P, 8) == 1 && bp_windows_in_range(P, 64)) {
+        // dense data: detector pairs, one 8-byte gather per (pixel, angle)
+        row_pair_kernel<<<dim3((P.D + 255) / 256, P.a), 256, 0, stream>>>(P, sino, reinterpret_cast<float2 *>(scaled));
+        const dim3 grid((P.N + 31) / 32, (P.N + 63) / 64);
+        bp_tile_kernel<8, true, true, true, true><<<grid, 256, 0, stream>>>(P, L, scaled, sino, img);
+    } else if (scaled) {
         row_scale_kernel<<<dim3((P.D + 255) / 256, P.a), 256, 0, stream>>>(P, sino, scaled);
         if (P.a >= kBpManyAngles) launch_bp_pix<8, true>(P, L, scaled, sino, img, stream);
         else launch_bp_pix<4, true>(P, L, scaled, sino, img, stream);

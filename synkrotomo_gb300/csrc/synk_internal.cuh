@@ -334,8 +334,9 @@ int device_sms();
 cudaError_t launch_geometry(const float *angles, int a, AngleGeom *geom, cudaStream_t stream);
 cudaError_t launch_fp(const ProbGeom &P, const AngleLists &L, const float2 *xpair, const float2 *xTpair, float *sino,
                       cudaStream_t stream);
-// scaled: scratch of a*D floats for the lbase-scaled rows (faster inner loop),
-// or null for the unscaled kernel (no scratch)
+// scaled: scratch of 2*a*D floats for the lbase-scaled rows (faster inner
+// loop; detector pairs on the dense in-range path), or null for the unscaled
+// kernel (no scratch)
 cudaError_t launch_bp(const ProbGeom &P, const AngleLists &L, const float *sino, float *img, cudaStream_t stream,
                       float *scaled);
 // R, C and the lists of rays that only clip a corner pixel (their R stored
