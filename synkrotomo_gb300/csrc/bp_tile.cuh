@@ -60,8 +60,9 @@ __device__ __forceinline__ void bp_stage(const ProbGeom &P, int k0, BpStage &st)
 // SCALED: the sinogram rows of the staged (non-near-axis) angles are already
 // multiplied by their lbase (row_scale), which saves one multiply per
 // (pixel, angle); near-axis rows stay unscaled for bp_exact_angles.
-// UNR = 2 walks the angles in pairs, so that both angles' gathers are in flight
-// together; the sums stay in angle order, bit for bit those of UNR = 1.
+// UNR = 2 (4) walks the angles two (four) at a time, so that their gathers
+// are in flight together; the sums stay in angle order, bit for bit those of
+// UNR = 1.
 // PAIR (INRANGE only): sino holds detector pairs, entry s of row k =
 // (row[s], row[s+1]) at float offset 2*(k*D + s), so one 8-byte gather serves
 // both candidates (the same values, the same sums).
@@ -146,7 +147,14 @@ __device__ __forceinline__ void bp_chunk(const ProbGeom &P, const BpStage &st, i
         }
     };
     int i = kphase;
-    if constexpr (UNR == 2)
+    if constexpr (UNR == 4)
+        for (; i + 3 * kstride < nk; i += 4 * kstride) {
+            angle(i);
+            angle(i + kstride);
+            angle(i + 2 * kstride);
+            angle(i + 3 * kstride);
+        }
+    if constexpr (UNR >= 2)
         for (; i + kstride < nk; i += 2 * kstride) {
             angle(i);
             angle(i + kstride);

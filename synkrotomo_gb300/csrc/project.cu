@@ -509,8 +509,11 @@ constexpr int kBpManyAngles = 256;     // angle count from which the 8-pixel var
 
 // sino_s: the fast-path rows (scaled when SCALED, else sino itself); sino:
 // the unscaled rows read by the near-axis angles.
+// PAIR (the dense in-range path) walks the angles four at a time with 64
+// registers (4 blocks per SM): 4.52 -> 4.14 ms at N = 2048, 2048 angles
+// (two at a time with 48 registers and 5 blocks: 4.52; two with 64: 4.33).
 template <int kBpPix, bool UNIT, bool INRANGE, bool SCALED, bool PAIR = false>
-__global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_tile_kernel(ProbGeom P, AngleLists L,
+__global__ void __launch_bounds__(256, PAIR ? 4 : BpShape<kBpPix>::kMinBlocks) bp_tile_kernel(ProbGeom P, AngleLists L,
                                                                    const float *__restrict__ sino_s,
                                                                    const float *__restrict__ sino,
                                                                    float *__restrict__ out) {
@@ -530,7 +533,7 @@ __global__ void __launch_bounds__(256, BpShape<kBpPix>::kMinBlocks) bp_tile_kern
         float part[kBpPix];
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) part[m] = 0.0f;
-        bp_chunk<kBpPix, UNIT, INRANGE, SCALED, 2, PAIR>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
+        bp_chunk<kBpPix, UNIT, INRANGE, SCALED, PAIR ? 4 : 2, PAIR>(P, st, kc, P.a, 0, 1, sino_s, xc, yc0, 8.0f, part);
 #pragma unroll
         for (int m = 0; m < kBpPix; ++m) comp_add(sum[m], comp[m], part[m]);
     }
