@@ -384,6 +384,14 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         fill_i32_kernel<<<(unsigned)((q.nslices + 255) / 256), 256, 0, st>>>(stop_iter, q.nslices, INT_MAX);
         SYNK_CUDA(cudaGetLastError(), "fill kernel");
         h.P = make_geom(q.a, q.rhozero, q.deltarho, q.numrhos, q.size, geom);
+        // the backprojection-grid backward phase (one large problem, every
+        // window of its 64-row tiles in range) reads rr as detector pairs
+        float *rrp = nullptr;
+        if (stack && bp_windows_in_range(h.P, 64)) {
+            SYNK_CUDA(sc.get(&rrp, 2 * pr * q.nslices), "cudaMallocAsync(residual pairs)");
+            SYNK_CUDA(cudaMemsetAsync(rrp, 0, sizeof(float) * 2 * pr * q.nslices, st), "memset");
+        }
+        h.rrp = rrp;
         SYNK_CUDA(make_setup(sc, q.angles, h.P, &h.L, st), "setup kernel");
         SYNK_CUDA(launch_normalisers(h.P, R, C, graze, glen, goff, graze_tmp, glen_tmp, gcnt, graze_capc, st),
                   "normaliser kernels");
@@ -496,7 +504,8 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
             if (stack) SYNK_CUDA(launch_sirt_fp_stack(host[0], it, sp.tol2, sp.record_final, st), "SIRT forward phase");
             else SYNK_CUDA(launch_sirt_fp_phase(sp, it, fpg, st), "SIRT forward phase");
             if (it == max_iter) break;
-            SYNK_CUDA(launch_sirt_bp_phase(sp, it, active, bpg, st), "SIRT backward phase");
+            if (host[0].rrp) SYNK_CUDA(launch_sirt_bp_stack(host[0], it, sp.tol2, active, st), "SIRT backward phase");
+            else SYNK_CUDA(launch_sirt_bp_phase(sp, it, active, bpg, st), "SIRT backward phase");
             // every 16 iterations, end the loop once no slice updates any more
             if (can_poll && (it & 15) == 15) {
                 int h_active = 1;

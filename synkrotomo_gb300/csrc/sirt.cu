@@ -116,11 +116,14 @@ __device__ __forceinline__ bool fp_needed(const SirtParams &p, const SirtProblem
 }
 // BP (the update) of iteration it: the slice is below its count and neither
 // stopped before nor converged at x_it.
-__device__ __forceinline__ bool bp_needed(const SirtParams &p, const SirtProblem &q, int s, int it) {
+__device__ __forceinline__ bool bp_needed(double tol2, const SirtProblem &q, int s, int it) {
     if (it >= q.iterations) return false;
-    if (p.tol2 <= 0.0) return true;
+    if (tol2 <= 0.0) return true;
     if (stop_of(q, s) < it) return false;
-    return !(res2_of(q, s, it) <= p.tol2 * q.b2[s]);
+    return !(res2_of(q, s, it) <= tol2 * q.b2[s]);
+}
+__device__ __forceinline__ bool bp_needed(const SirtParams &p, const SirtProblem &q, int s, int it) {
+    return bp_needed(p.tol2, q, s, it);
 }
 
 // Next item of a phase: static (block + i*grid) or from the phase's counter.
@@ -154,8 +157,14 @@ __device__ __forceinline__ double residual(const SirtProblem &q, int s, int k, i
     const size_t ray = (size_t)k * q.P.D + r;
     const float Rk = q.R[ray];
     if (Rk < 0.0f) return 0.0;
-    const float e = __fsub_rn(q.b[(size_t)s * pr + ray], fpv);
-    q.rr[(size_t)s * pr + ray] = __fmul_rn(__fmul_rn(Rk, e), row_scale(q.P.geom, k));
+    const size_t i = (size_t)s * pr + ray;
+    const float e = __fsub_rn(q.b[i], fpv);
+    const float v = __fmul_rn(__fmul_rn(Rk, e), row_scale(q.P.geom, k));
+    q.rr[i] = v;
+    if (q.rrp) {                                      // pair entries r (first half) and r-1 (second half)
+        q.rrp[2 * i] = v;
+        if (r > 0) q.rrp[2 * i - 1] = v;
+    }
     return (double)e * (double)e;
 }
 
@@ -560,6 +569,101 @@ __global__ void __launch_bounds__(256, 4) sirt_bp_phase_kernel(SirtParams p, int
         if (threadIdx.x == 0) *active = sh.any;
     }
     bp_phase(p, it, nullptr, sh);
+}
+
+// Backward phase of the split engine for one large problem (a slice stack)
+// on the standalone backprojector's grid: a block = 32 columns x 64 rows of
+// one slice (blockIdx.z), 8 rows per thread, the weighted residual read as
+// detector pairs (one 8-byte gather per pixel and angle), four angles at a
+// time, and the SIRT update x + C*bp (SIRT.fut:38-39) with both padded
+// copies of the iterate in the epilogue.  The angles are summed in the order
+// of bp_phase; a pixel's detector coordinate comes from its thread's first
+// row, so the iterates equal the generic phase's to rounding.  Block (0,0,0)
+// also applies the stopping rule of iteration it (sirt_bp_phase_kernel's rule).
+__global__ void __launch_bounds__(256, 4) sirt_bp_stack_kernel(SirtProblem q, int it, double tol2, int *active) {
+    __shared__ BpStage st;
+    __shared__ float tile[32][65];
+    __shared__ int any;
+    const int s = blockIdx.z;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) {
+        if (threadIdx.x == 0) any = 0;
+        __syncthreads();
+        int cnt = 0;
+        for (int z = threadIdx.x; z < q.nslices; z += blockDim.x) {
+            if (bp_needed(tol2, q, z, it)) ++cnt;
+            else if (tol2 > 0.0 && it < q.iterations && stop_of(q, z) > it) q.stop_iter[z] = it;
+        }
+        if (cnt) atomicAdd(&any, cnt);
+        __syncthreads();
+        if (threadIdx.x == 0) *active = any;
+    }
+    if (!bp_needed(tol2, q, s, it)) return;              // block-uniform
+    const ProbGeom &P = q.P;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int col = blockIdx.x * 32 + lane;
+    const int row0 = blockIdx.y * 64 + warp;
+    const float xc = (float)(col - P.half) + 0.5f;
+    const float yc0 = (float)(row0 - P.half) + 0.5f;
+    const size_t pr = (size_t)P.a * P.D, np = (size_t)P.N * (P.N + 2);
+    const float *rows = q.rrp + (size_t)s * pr * 2;
+    float sum[8], comp[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) sum[m] = comp[m] = 0.0f;
+    for (int kc = 0; kc < P.a; kc += kBpChunk) {
+        __syncthreads();
+        bp_stage(P, kc, st);
+        __syncthreads();
+        float part[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) part[m] = 0.0f;
+        bp_chunk<8, true, true, true, 4, true>(P, st, kc, P.a, 0, 1, rows, xc, yc0, 8.0f, part);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) comp_add(sum[m], comp[m], part[m]);
+    }
+    float ex[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) ex[m] = 0.0f;
+    bp_exact_angles<8>(P, q.L.exact, __ldg(q.L.counts + 2), 0, 1, q.rr + (size_t)s * pr, row0, 8, col, ex);
+    float *xpad = q.xpad + (size_t)s * np;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        float bpv = (sum[m] + comp[m]) + ex[m];
+        const int row = row0 + 8 * m;
+        // the image corners add the terms of the rays that clip only them
+        // (warp-uniform tests: the warp of a corner row sums them)
+        if (row == 0 || row == P.N - 1) {
+            const int cb = row == P.N - 1 ? 2 : 0;
+            if (blockIdx.x == 0) {
+                const float t = corner_terms_warp(q, s, cb);
+                if (col == 0) bpv = __fadd_rn(bpv, t);
+            }
+            if (blockIdx.x == gridDim.x - 1) {
+                const float t = corner_terms_warp(q, s, cb + 1);
+                if (col == P.N - 1) bpv = __fadd_rn(bpv, t);
+            }
+        }
+        float xi = 0.0f;
+        if (row < P.N && col < P.N) {
+            float *xp = xpad + (size_t)row * (P.N + 2) + col + 1;
+            xi = __fadd_rn(*xp, __fmul_rn(q.C[(size_t)row * P.N + col], bpv));      // SIRT.fut:38-39
+            *xp = xi;
+        }
+        tile[lane][warp + 8 * m] = xi;
+    }
+    __syncthreads();
+    // transposed write: xTpad[col][row + 1] for the tile's 32 columns x 64 rows
+    float *xTpad = q.xTpad + (size_t)s * np;
+    for (int i = threadIdx.x; i < 32 * 64; i += blockDim.x) {
+        const int cl = i >> 6, rl = i & 63;
+        const int c = blockIdx.x * 32 + cl, r = blockIdx.y * 64 + rl;
+        if (c < P.N && r < P.N) xTpad[(size_t)c * (P.N + 2) + r + 1] = tile[cl][rl];
+    }
+}
+
+cudaError_t launch_sirt_bp_stack(const SirtProblem &q, int it, double tol2, int *active, cudaStream_t stream) {
+    const dim3 grid((q.P.N + 31) / 32, (q.P.N + 63) / 64, q.nslices);
+    sirt_bp_stack_kernel<<<grid, 256, 0, stream>>>(q, it, tol2, active);
+    return cudaGetLastError();
 }
 
 // Per-problem item counts and begin offsets (depend on the angle lists).

@@ -20,6 +20,8 @@ struct SirtProblem {
     float *xpad;          // [nslices][N][N+2] iterate, zero column on each side
     float *xTpad;         // [nslices][N][N+2] transposed iterate, same padding
     float *rr;            // [nslices][a*D] weighted residual R*(b - FP(x))
+    float *rrp;           // [nslices][a*D] its detector pairs (rr[s], rr[s+1]) per row (0 past the row end)
+                          // for the backprojection-grid backward phase; null when that phase does not run
     double *res2;         // [nslices][iterations+1] sum of (b - FP(x_k))^2
     const double *b2;     // [nslices] ||b||^2
     int *stop_iter;       // [nslices] iteration at which the stopping rule fired (init: INT_MAX)
@@ -64,6 +66,9 @@ cudaError_t launch_sirt_fp_phase(const SirtParams &p, int it, int grid, cudaStre
 cudaError_t launch_sirt_bp_phase(const SirtParams &p, int it, int *active, int grid, cudaStream_t stream);
 // forward phase of the split engine for one problem (a slice stack): the projector's grid, residual epilogue
 cudaError_t launch_sirt_fp_stack(const SirtProblem &q, int it, double tol2, int record_final, cudaStream_t stream);
+// backward phase of the split engine for one problem on the backprojector's tile grid (needs q.rrp and every
+// detector window of its 64-row tiles inside the sinogram); block (0,0,0) applies the stopping rule into *active
+cudaError_t launch_sirt_bp_stack(const SirtProblem &q, int it, double tol2, int *active, cudaStream_t stream);
 cudaError_t launch_sirt_finalize(SirtProblem *probs, int nprob, int max_slices, int record_final,
                                  cudaStream_t stream);
 

@@ -166,11 +166,14 @@ def test_phase_split_engine_uneven_batch(gpu):
 
 
 def test_phase_split_engine_large_stack_matches_persistent(gpu):
-    """Above 6e7 work per iteration a single problem's forward phase runs on the
-    projector's grid (sirt_fp_stack_kernel): with the same work splits the
-    per-ray values are the same, so the iterates equal the persistent kernel's
-    bit for bit.  With the splits each engine picks for its own grid the sums
-    run in another order and the iterates agree to rounding."""
+    """Above 6e7 work per iteration a single problem runs on the projectors'
+    grids: the forward phase in sirt_fp_stack_kernel (the per-ray values of
+    the generic phase) and the backward phase in sirt_bp_stack_kernel (32 x 64
+    pixel tiles, the residual as detector pairs, the same angle order).  A
+    pixel's detector coordinate comes from its thread's first row, so the
+    iterates agree with the persistent kernel's to rounding, slice by slice,
+    and with the oracle; with a stopping rule every slice stops at the same
+    iteration."""
     size, a, ns, its = 256, 180, 4, 12
     g = phantom.geometry(size, a)
     vol = phantom.ellipsoid_volume(size, ns, seed=5)
@@ -178,17 +181,26 @@ def test_phase_split_engine_large_stack_matches_persistent(gpu):
                       for i in range(ns)])
     ang, bd = _dev(g.angles), _dev(sinos.ravel())
     assert ns * a * size * (size + g.numrhos) > 6e7
-    for fs, bs in ((2, 4), (8, 1)):
+    for fs, bs in ((2, 4), (8, 1), (0, 0)):
         xp, rp, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
                                    fp_split=fs, bp_split=bs, grid_blocks=rt.resident_blocks())
         xs, rs, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
                                    fp_split=fs, bp_split=bs, grid_blocks=-1)
-        assert torch.equal(xp, xs), (fs, bs)
-        np.testing.assert_allclose(rs.cpu().numpy(), rp.cpu().numpy(), rtol=1e-12)
-    xp, _, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its,
-                              grid_blocks=rt.resident_blocks())
-    xs, rs, _ = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, residuals=True,
-                               grid_blocks=-1)
-    assert rel_l2(xs.cpu().numpy(), xp.cpu().numpy()) < 1e-6
+        xp_, xs_ = xp.cpu().numpy().reshape(ns, -1), xs.cpu().numpy().reshape(ns, -1)
+        for z in range(ns):
+            assert rel_l2(xs_[z], xp_[z]) < 1e-6, (fs, bs, z)
+        np.testing.assert_allclose(rs.cpu().numpy(), rp.cpu().numpy(), rtol=1e-5)
     ref = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), sinos[1], its)
     assert rel_l2(xs.cpu().numpy().reshape(ns, -1)[1], ref) < 1e-5
+    hist = rp.cpu().numpy()
+    tol = float(np.median(hist[:, 6])) * 1.003
+    _, _, dp = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, tol=tol,
+                              grid_blocks=rt.resident_blocks())
+    xs2, _, ds = rt.sirt_slices(ang, g.rhozero, g.deltarho, g.numrhos, size, ns, None, bd, its, tol=tol,
+                                grid_blocks=-1)
+    assert torch.equal(dp, ds)
+    assert int(ds.min()) < its
+    for z in range(ns):
+        k = int(ds[z].item())
+        refk = cpu_ref.sirt(g.angles, g.rhozero, g.deltarho, np.zeros(size * size, np.float32), sinos[z], k)
+        assert rel_l2(xs2.cpu().numpy().reshape(ns, -1)[z], refk) < 1e-5, z
