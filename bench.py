@@ -376,31 +376,67 @@ def run_sirt_cfg0(dev):
     return out
 
 
-def run_sirt3d_sharded(dev, world, slices_per_rank=8, iterations=20, seed=0):
-    """The slice stack's geometry (512 x 512 slices, 360 angles, 725
-    detectors, 1 % noise) split over the ranks by shard.sirt3d_sharded
-    (contiguous slice ranges, one SIRT launch per rank, one all-gather of the
-    results at the end): slices_per_rank slices per rank (weak scaling),
-    iterations updates each.  Returns the slowest rank's milliseconds and the
-    whole job's slice-iterations per second."""
+def _ellipsoid_stack_gpu(size, n_slices, seed, dev, n_ellipsoids=12):
+    """phantom.ellipsoid_volume's stack (the same seeded ellipsoids and rule),
+    evaluated on the GPU in float64: [n_slices, size*size] float32."""
+    import math
+
+    import torch
+
+    rng = np.random.default_rng(seed)
+    half, zh = size / 2.0, n_slices / 2.0
+    coords = torch.arange(size, dtype=torch.float64, device=dev) - half + 0.5
+    y, x = torch.meshgrid(coords, coords, indexing="ij")
+    params = []
+    for _ in range(n_ellipsoids):
+        cx, cy = rng.uniform(-0.6, 0.6, 2) * half
+        cz = rng.uniform(-0.6, 0.6) * zh
+        ax, ay = rng.uniform(0.05, 0.4, 2) * half
+        az = rng.uniform(0.05, 0.4) * zh
+        phi = rng.uniform(0.0, math.pi)
+        val = rng.uniform(0.0, 1.0)
+        params.append((cx, cy, cz, ax, ay, az, math.cos(phi), math.sin(phi), val))
+    vol = torch.zeros(n_slices, size, size, dtype=torch.float32, device=dev)
+    for z in range(n_slices):
+        zc = z - zh + 0.5
+        sl = torch.zeros(size, size, dtype=torch.float64, device=dev)
+        for cx, cy, cz, ax, ay, az, c, s_, val in params:
+            dz = ((zc - cz) / az) ** 2
+            if dz > 1.0:
+                continue
+            u = (x - cx) * c + (y - cy) * s_
+            v = -(x - cx) * s_ + (y - cy) * c
+            sl += (((u / ax) ** 2 + (v / ay) ** 2) <= 1.0 - dz).to(torch.float64) * val
+        vol[z] = sl.to(torch.float32)
+    return vol.reshape(n_slices, size * size)
+
+
+def run_sirt3d_sharded(dev, world, slices=512, iterations=10, seed=0):
+    """The slice stack of the SIRT3D configuration (512 slices of 512 x 512,
+    360 angles, 725 detectors, 1 % noise) split over the ranks by
+    shard.sirt3d_sharded (contiguous slice ranges, one SIRT launch per rank,
+    one all-gather of the results at the end): all slices, `iterations`
+    updates each (strong scaling: the stack is fixed).  Returns the slowest
+    rank's milliseconds and the whole job's slice-iterations per second."""
     import torch
 
     from synkrotomo_gb300 import phantom, shard
     from synkrotomo_gb300 import runtime as rt
 
     N, a, D = 512, 360, 725
-    ns = slices_per_rank * world
+    ns = int(slices)
     g = phantom.geometry(N, a, numrhos=D)
     ang = torch.from_numpy(g.angles).to(dev)
     rhos = torch.from_numpy((np.float32(g.rhozero) + np.arange(D, dtype=np.float32)).astype(np.float32)).to(dev)
-    vol = phantom.ellipsoid_volume(N, ns, seed)
-    sinos = []
+    vol = _ellipsoid_stack_gpu(N, ns, seed, dev)
+    proj = torch.empty(ns * a * D, dtype=torch.float32, device=dev)
     for z in range(ns):     # every rank makes the same stack (same seeds)
-        b = rt.forwardprojection(ang, g.rhozero, g.deltarho, D, torch.from_numpy(vol[z]).to(dev))
+        b = proj[z * a * D:(z + 1) * a * D]
+        rt.forwardprojection(ang, g.rhozero, g.deltarho, D, vol[z], out=b)
         gen = torch.Generator(device=dev).manual_seed(seed * 1000 + z)
-        sinos.append(b + torch.randn(b.shape, device=dev, generator=gen) * (0.01 * float(b.max())))
-    proj = torch.cat(sinos)
-    shard.sirt3d_sharded(ang, rhos, proj, 2, N, nslices=ns)          # warm-up
+        b += torch.randn(b.shape, device=dev, generator=gen) * (0.01 * float(b.max()))
+    del vol
+    shard.sirt3d_sharded(ang, rhos, proj, 1, N, nslices=ns)          # warm-up
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -412,8 +448,9 @@ def run_sirt3d_sharded(dev, world, slices_per_rank=8, iterations=20, seed=0):
     torch.cuda.synchronize()
     ms = shard.max_over_ranks(e0.elapsed_time(e1))
     assert volr.numel() == ns * N * N
-    return {"slices": ns, "slices_per_rank": slices_per_rank, "iterations": iterations, "ranks": world,
-            "ms": ms, "slice_iterations_per_s": ns * iterations / (ms * 1e-3),
+    return {"slices": ns, "slices_per_rank": -(-ns // world), "iterations": iterations, "ranks": world,
+            "ms": ms, "us_per_slice_iteration": 1e3 * ms * world / (ns * iterations),
+            "slice_iterations_per_s": ns * iterations / (ms * 1e-3), "scaling": "strong",
             "split": "contiguous slice ranges, one all-gather of the results"}
 
 

@@ -6,6 +6,8 @@ import os
 import subprocess
 import sys
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -75,3 +77,14 @@ def test_clock_summary_reads_the_samples_of_the_timed_region():
     assert cs.summary()["sm_mhz"] == 1200.0
     cs.lines, cs.start = [], 0
     assert cs.summary()["reasons"] == ["unsampled"]
+
+
+def test_bench_stack_generator_matches_phantom():
+    """The bench's device-side slice-stack generator evaluates
+    phantom.ellipsoid_volume's seeded ellipsoids with the same rule."""
+    import bench
+    import torch
+    from synkrotomo_gb300 import phantom
+    for size, ns, seed in ((32, 9, 3), (48, 12, 0)):
+        got = bench._ellipsoid_stack_gpu(size, ns, seed, torch.device("cpu")).numpy()
+        np.testing.assert_array_equal(got, phantom.ellipsoid_volume(size, ns, seed))
