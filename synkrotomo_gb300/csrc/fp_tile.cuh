@@ -1,11 +1,13 @@
 // Ray-driven forward projection with one lane per angle, shared by the
 // standalone forward projector and the SIRT kernels.
 //
-// A warp owns one detector index r and 32 angles of the same class (all steep
-// or all flat, none near-axis).  The 32 rays of neighbouring angles at the
-// same detector cross almost the same pixels of a frame row, so each gather of
-// a row touches 2-3 sectors (lanes on adjacent detectors of one angle would
-// span ~45 columns).  Two image layouts:
+// A lane owns one ray (detector r, angle k); the lanes of a warp hold
+// neighbouring rays of the same class (all steep or all flat, none
+// near-axis): 32 angles at one detector, or 4 angles x 8 detectors in the
+// standalone projector.  Neighbouring rays cross almost the same pixels of a
+// frame row, so each gather of a row touches few sectors (32 adjacent
+// detectors of one angle would span ~45 columns; 4 x 8 averages fewest).  The
+// walk takes the warp's union of the lanes' row ranges.  Two image layouts:
 //   fp_lane_ray_pair (standalone projector): pair images, entry i of a row =
 //     (pixel i-1, pixel i - pixel i-1) with zeros outside the image and a zero
 //     entry ending the row; one unconditional 8-byte gather per row step.
