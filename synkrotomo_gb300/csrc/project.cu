@@ -532,8 +532,12 @@ __global__ void __launch_bounds__(256, PAIR ? 4 : BpShape<kBpPix>::kMinBlocks) b
                                                                    float *__restrict__ out) {
     __shared__ BpStage st;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int col = blockIdx.x * 32 + lane;
-    const int row0 = blockIdx.y * (8 * kBpPix) + warp;
+    // PAIR: a warp's lanes are 8 columns x 4 rows of the tile (rows 8 apart per
+    // pixel m as before), so one angle's gathers of a warp span fewer
+    // detectors than 32 columns of one row (4.15 -> 4.09 ms; 16 x 2: 4.11)
+    const int col = PAIR ? blockIdx.x * 32 + (warp & 3) * 8 + (lane & 7) : blockIdx.x * 32 + lane;
+    const int row0 = PAIR ? blockIdx.y * (8 * kBpPix) + (warp >> 2) * 4 + (lane >> 3)
+                          : blockIdx.y * (8 * kBpPix) + warp;
     const float xc = (float)(col - P.half) + 0.5f;
     const float yc0 = (float)(row0 - P.half) + 0.5f;
     float sum[kBpPix], comp[kBpPix];
