@@ -3,7 +3,7 @@
 //
 // A block of 256 threads owns a tile of 32 columns; thread (lane, warp) owns
 // column lane and PIX rows spaced RSTEP apart.  The per-angle constants of
-// the chord-length trapezoid are staged in shared memory 64 angles at a time
+// the chord-length trapezoid are staged in shared memory kBpChunk angles at a time
 // and read as one broadcast float4 + one float2 per angle; each (pixel, angle)
 // then costs ~14 FP32/INT instructions and two sinogram gathers:
 //   q    = x_c*cos - y_c*sin - rz_c               (rho of the centre from the middle
@@ -22,7 +22,11 @@
 
 namespace synk {
 
-constexpr int kBpChunk = 64;
+// Angles per staged chunk (and per partial sum before the compensated
+// total).  128 rather than 64: half the staging barriers, the whole angle set
+// of N=128 problems in one chunk (SIRT at N=128, 200 iterations: 4.08 -> 3.96
+// ms; dense backprojection 4.09 -> 4.07 ms).
+constexpr int kBpChunk = 128;
 
 struct BpStage {
     float4 cs[kBpChunk];   // cos, sin, h/b, 1/b

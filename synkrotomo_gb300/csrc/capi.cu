@@ -34,6 +34,8 @@ struct synk_context {
     cudaStream_t stream = nullptr;
     std::string err;
     int *d_status = nullptr;   // written by persistent kernels (SYNK_ETIMEOUT)
+    int *h_poll = nullptr;     // pinned: active-slice counts read back by the SIRT loop's stopping rule
+    cudaEvent_t poll_ev[2] = {nullptr, nullptr};
     unsigned long long barrier_timeout_ns = 2000000000ull;
     unsigned barrier_extra = 0;   // fault injection: blocks a grid barrier waits for that never come
 };
@@ -500,18 +502,32 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusNone;
         const bool can_poll = sp.tol2 > 0.0 && !staging && cap == cudaStreamCaptureStatusNone;
+        int poll_slot = 0, poll_prev = -1;
         for (int it = 0; it <= max_iter; ++it) {
             if (stack) SYNK_CUDA(launch_sirt_fp_stack(host[0], it, sp.tol2, sp.record_final, st), "SIRT forward phase");
             else SYNK_CUDA(launch_sirt_fp_phase(sp, it, fpg, st), "SIRT forward phase");
             if (it == max_iter) break;
             if (host[0].rrp) SYNK_CUDA(launch_sirt_bp_stack(host[0], it, sp.tol2, active, st), "SIRT backward phase");
             else SYNK_CUDA(launch_sirt_bp_phase(sp, it, active, bpg, st), "SIRT backward phase");
-            // every 16 iterations, end the loop once no slice updates any more
+            // Every 16 iterations the count of slices still updating is copied
+            // to pinned memory behind the backward phase, and the host waits
+            // for the copy queued 16 iterations earlier, not for the stream:
+            // the GPU keeps the iterations in between queued (the chained
+            // launches stay chained) and the loop ends once no slice updates
+            // any more.  The at most 16-31 iterations already queued then skip
+            // their work in the kernels (stopping rule per slice).  Draining
+            // the stream at each check cost more than stopping saved (N=128:
+            // 184 iterations to the residual 4.20 ms, 200 iterations 3.96 ms).
             if (can_poll && (it & 15) == 15) {
-                int h_active = 1;
-                SYNK_CUDA(cudaMemcpyAsync(&h_active, active, sizeof(int), cudaMemcpyDeviceToHost, st), "read active");
-                SYNK_CUDA(cudaStreamSynchronize(st), "read active");
-                if (h_active == 0) break;
+                SYNK_CUDA(cudaMemcpyAsync(ctx->h_poll + poll_slot, active, sizeof(int), cudaMemcpyDeviceToHost, st),
+                          "read active");
+                SYNK_CUDA(cudaEventRecord(ctx->poll_ev[poll_slot], st), "record poll");
+                if (poll_prev >= 0) {
+                    SYNK_CUDA(cudaEventSynchronize(ctx->poll_ev[poll_prev]), "wait poll");
+                    if (ctx->h_poll[poll_prev] == 0) break;
+                }
+                poll_prev = poll_slot;
+                poll_slot ^= 1;
             }
         }
     } else {
@@ -571,8 +587,11 @@ int synk_context_new(synk_context **out, int device, void *stream) {
     ctx->device = device;
     ctx->stream = static_cast<cudaStream_t>(stream);
     if (cudaMalloc(&ctx->d_status, sizeof(int)) != cudaSuccess ||
-        cudaMemset(ctx->d_status, 0, sizeof(int)) != cudaSuccess) {
-        delete ctx;
+        cudaMemset(ctx->d_status, 0, sizeof(int)) != cudaSuccess ||
+        cudaHostAlloc(&ctx->h_poll, 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->poll_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->poll_ev[1], cudaEventDisableTiming) != cudaSuccess) {
+        synk_context_free(ctx);
         return SYNK_ENOMEM;
     }
     *out = ctx;
@@ -584,6 +603,9 @@ void synk_context_free(synk_context *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_status);
+    if (ctx->h_poll) cudaFreeHost(ctx->h_poll);
+    for (cudaEvent_t e : ctx->poll_ev)
+        if (e) cudaEventDestroy(e);
     delete ctx;
 }
 

@@ -28,14 +28,15 @@ namespace synk {
 // Rows per partial sum of a ray before it enters the compensated (Neumaier)
 // total: plain float32 within a chunk, compensated across chunks.  Longer
 // chunks mean fewer compensation steps and a tighter row loop; measured at
-// N=2048 / 2048 angles, the standalone projector takes 4.54 / 4.34 / 4.22 ms
-// with 32 / 64 / 128 rows, and the SIRT slice stack (N=512, 360 angles)
-// 107.8 / 106.7 us per slice-iteration with 32 / 64.  A float32 partial sum
-// of n terms errs by at most (n - 1) * 2^-24 of the terms' absolute sum, so
-// 128 rows stay far inside the 1e-5 parity bar, and a 2048-row ray still
-// gets 16 compensated chunks.
-constexpr int kPairCompRows = 128;
-constexpr int kSirtCompRows = 64;
+// N=2048 / 2048 angles, the standalone projector takes 4.54 / 4.34 / 4.22 /
+// 4.17 ms with 32 / 64 / 128 / 256 rows, and the SIRT slice stack (N=512,
+// 360 angles) 107.8 / 106.7 / 105.8 us per slice-iteration with 32 / 64 /
+// 128 (the last with 128-angle backprojection chunks).  A float32 partial
+// sum of n terms errs by at most (n - 1) * 2^-24 of the terms' absolute sum,
+// so 256 rows stay far inside the 1e-5 parity bar, and a 2048-row ray still
+// gets 8 compensated chunks.
+constexpr int kPairCompRows = 256;
+constexpr int kSirtCompRows = 128;
 
 // Angle order of the lane-per-angle projector (built by angle_lists_kernel):
 //   order[g*32 + lane]: angle of lane in group g, -1 for an idle lane;
