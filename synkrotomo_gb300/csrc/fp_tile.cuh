@@ -78,23 +78,43 @@ __device__ __forceinline__ float fp_ray_exact_f32(const ProbGeom &P, const Angle
     return acc;
 }
 
-// Sum over frame rows [jb, je) of detector r for the lane's angle k (k < 0:
-// idle lane, returns 0).  img_pad: padded frame image (stride N+2, pixel
-// (j, c) at j*(N+2) + c + 1).  All 32 lanes of the warp must call it.
-__device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, const float *__restrict__ img_pad,
-                                             int jb, int je) {
+// fp_lane_ray: the sum over frame rows [jb, je) of detector r for the lane's
+// angle k (k < 0: idle lane, returns 0) on the padded frame image, in two
+// parts.  lane_ray_prep reads only the problem's static tables (geometry,
+// detector positions), so a kernel can run it before waiting for the kernel
+// that writes the image; the walk's row range is the warp's union of the
+// lanes' ranges.  All 32 lanes of the warp must call both.
+struct LaneRay {
+    float x0, slope, ainv, lbase;
+    int J0, J1;
+    bool valid;
+};
+
+__device__ __forceinline__ LaneRay lane_ray_prep(const ProbGeom &P, int k, int r, int jb, int je) {
     const AngleGeom g = load_geom(P.geom, k >= 0 ? k : 0);
     const float rho = __fadd_rn(P.rhozero, __fmul_rn((float)r, P.deltarho));    // forwardprojection.fut:28
     const float intercept = __fdiv_rn(rho, g.cost);                               // forwardprojection.fut:29
-    const float x0 = ray_x0(g, intercept);
+    LaneRay L;
+    L.x0 = ray_x0(g, intercept);
     int j0 = 0, j1 = 0;
-    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, x0, j0, j1);
+    if (k >= 0 && !(fabsf(rho) > 0.75f * (float)P.N + 2.0f)) lane_rows(P, g, L.x0, j0, j1);
     j0 = max(j0, jb);
     j1 = min(j1, je);
     if (j1 <= j0) { j0 = je; j1 = je; }
-    const int J0 = __reduce_min_sync(0xffffffffu, j0);
-    const int J1 = __reduce_max_sync(0xffffffffu, j1);
-    const float slope = g.slope, ainv = g.ainv;
+    L.J0 = __reduce_min_sync(0xffffffffu, j0);
+    L.J1 = __reduce_max_sync(0xffffffffu, j1);
+    L.slope = g.slope;
+    L.ainv = g.ainv;
+    L.lbase = g.lbase;
+    L.valid = k >= 0;
+    return L;
+}
+
+// The walk of a prepared ray over the padded frame image img_pad (stride N+2,
+// pixel (j, c) at j*(N+2) + c + 1); returns 0 for an idle lane.
+__device__ __forceinline__ float fp_lane_walk(const ProbGeom &P, const LaneRay &L, const float *__restrict__ img_pad) {
+    const float x0 = L.x0, slope = L.slope, ainv = L.ainv;
+    const int J0 = L.J0, J1 = L.J1;
     const int stride = P.N + 2;
     const unsigned lim = (unsigned)P.N;     // c + 1 in [0, N]
     const int half = P.half;
@@ -128,7 +148,13 @@ __device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, co
         for (; j < jend; ++j, jf += 1.0f) row(fmaf(jf, slope, x0), j, part);
         comp_add(sum, comp, part);
     }
-    return k >= 0 ? (sum + comp) * g.lbase : 0.0f;
+    return L.valid ? (sum + comp) * L.lbase : 0.0f;
+}
+
+__device__ __forceinline__ float fp_lane_ray(const ProbGeom &P, int k, int r, const float *__restrict__ img_pad,
+                                             int jb, int je) {
+    const LaneRay L = lane_ray_prep(P, k, r, jb, je);
+    return fp_lane_walk(P, L, img_pad);
 }
 
 // fp_lane_ray on a pair image: pair[j*(N+2) + i] = (pad(j, i), pad(j, i+1) -

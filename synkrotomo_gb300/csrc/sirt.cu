@@ -254,6 +254,22 @@ __device__ __forceinline__ void row_part(int N, int S, int part, int &jb, int &j
 }
 
 // ---- phase FP of iteration `it` ------------------------------------------------
+// Programmatic dependent launch: a phase kernel launched with programmatic
+// stream serialization lets the next one be scheduled once all of its blocks
+// have started (launch_dependents), and the next one's blocks wait in
+// griddepcontrol.wait until this grid has completed and its writes are
+// visible.  Every block waits before it reads anything an earlier kernel
+// wrote, and before it exits, so completion stays transitive along the chain.
+// Launched without the attribute both instructions return at once.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// CHAINED (the chained phase kernel): the item's static setup (decode, the
+// rays' geometry and row ranges, the backprojection's first angle chunk)
+// runs before griddepcontrol.wait, while the previous phase finishes; every
+// read of data an earlier kernel of the loop wrote (the iterate, rr, the
+// residual sums, the stop iterations) comes after it.
+template <bool CHAINED>
 __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtShared &sh) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long total = p.totals[0];
@@ -272,7 +288,6 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
             cur = &q;
             cur_slice = s;
         }
-        if (!fp_needed(p, q, s, it)) continue;            // uniform over the block
         const int S = q.fp_split, lgS = __ffs(S) - 1, G = 8 >> lgS;
         const int ngroups = __ldg(q.L.counts) + __ldg(q.L.counts + 1);
         const int nsteep = __ldg(q.L.counts);
@@ -289,8 +304,11 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
             // S = 1: 4 angles x 8 detectors per warp (as sirt_fp_stack_kernel)
             const int r = S == 1 ? db * 8 + (lane & 7) : db * G + (warp >> lgS);
             const int k = r < P.D ? __ldg(q.L.order + grp * 32 + (S == 1 ? warp * 4 + (lane >> 3) : lane)) : -1;
+            const LaneRay L = lane_ray_prep(P, k, r, jb, je);
+            if (CHAINED) chain_wait();
+            if (!fp_needed(p, q, s, it)) continue;        // uniform over the block
             const float *img = (grp < nsteep ? q.xpad : q.xTpad) + (size_t)s * np;
-            const float v = fp_lane_ray(P, k, r, img, jb, je);
+            const float v = fp_lane_walk(P, L, img);
             sh.red[warp][lane] = v;
             __syncthreads();
             if (part == 0 && k >= 0) {
@@ -299,6 +317,8 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
                 e2 = residual(q, s, k, r, fpv);
             }
         } else if (rem < fast_items + __ldg(q.L.counts + 2) * ((P.D + 7) / 8)) {
+            if (CHAINED) chain_wait();
+            if (!fp_needed(p, q, s, it)) continue;        // uniform over the block
             const int etiles = (P.D + 7) / 8;             // near-axis rays: one per warp
             const int x = rem - fast_items;
             const int e = x / etiles;
@@ -309,6 +329,8 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
                 if (lane == 0) e2 = residual(q, s, k, r, v);
             }
         } else {
+            if (CHAINED) chain_wait();
+            if (!fp_needed(p, q, s, it)) continue;        // uniform over the block
             // corner-clipping rays: one per warp
             const int gidx = (rem - fast_items - __ldg(q.L.counts + 2) * ((P.D + 7) / 8)) * 8 + warp;
             if (gidx < graze_count(q)) e2 = graze_ray(q, s, gidx);      // warp-uniform
@@ -322,7 +344,8 @@ __device__ void fp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
 // ---- phase BP of iteration `it` ------------------------------------------------
 // One item: a tile of 32 columns x PIX*(8/bp_split) rows of slice s; thread
 // (lane, warp) sums PIX rows of one column over its part of the angles.
-template <int PIX>
+// STAGED0: the caller already staged angle chunk 0 into sh.st.
+template <int PIX, bool STAGED0>
 __device__ __forceinline__ void bp_item(const SirtProblem &q, int s, int rem, SirtShared &sh) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const ProbGeom &P = q.P;
@@ -345,7 +368,7 @@ __device__ __forceinline__ void bp_item(const SirtProblem &q, int s, int rem, Si
     for (int m = 0; m < PIX; ++m) sum[m] = comp[m] = 0.0f;
     for (int kc = 0; kc < P.a; kc += kBpChunk) {
         __syncthreads();
-        bp_stage(P, kc, sh.st);
+        if (!STAGED0 || kc > 0) bp_stage(P, kc, sh.st);
         __syncthreads();
         float prt[PIX];
 #pragma unroll
@@ -403,6 +426,7 @@ __device__ __forceinline__ void bp_item(const SirtProblem &q, int s, int rem, Si
     }
 }
 
+template <bool CHAINED>
 __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtShared &sh) {
     const long long total = p.totals[1];
     for (long long item = next_item(p, counter, -1, sh); item < total; item = next_item(p, counter, item, sh)) {
@@ -410,11 +434,18 @@ __device__ void bp_phase(const SirtParams &p, int it, unsigned *counter, SirtSha
         const SirtProblem &q = p.probs[qi];
         int s, rem;
         item_slice(item - q.bp_begin, q.bp_ips, s, rem);
+        if (CHAINED) {
+            // the first angle chunk's constants are static: stage them while
+            // the forward phase finishes
+            __syncthreads();
+            bp_stage(q.P, 0, sh.st);
+            chain_wait();
+        }
         if (!bp_needed(p, q, s, it)) continue;            // uniform over the block
         switch (q.bp_pix) {                               // uniform over the block
-            case 1: bp_item<1>(q, s, rem, sh); break;
-            case 2: bp_item<2>(q, s, rem, sh); break;
-            default: bp_item<4>(q, s, rem, sh); break;
+            case 1: bp_item<1, CHAINED>(q, s, rem, sh); break;
+            case 2: bp_item<2, CHAINED>(q, s, rem, sh); break;
+            default: bp_item<4, CHAINED>(q, s, rem, sh); break;
         }
     }
 }
@@ -426,7 +457,7 @@ __global__ void __launch_bounds__(256, 3) sirt_persistent_kernel(SirtParams p) {
         // phase 2*it: FP.  Rotating counters: reset the one of the phase after next.
         const int ph = 2 * it;
         if (p.dynamic && blockIdx.x == 0 && threadIdx.x == 0) p.work[(ph + 1) % 3] = 0u;
-        fp_phase(p, it, p.work + ph % 3, sh);
+        fp_phase<false>(p, it, p.work + ph % 3, sh);
         if (!grid_barrier(p.bar, nb, p.status, p.timeout_ns, &sh.flag)) return;
         if (it == p.max_iterations) break;
         // stopping rule (identical decision in every block)
@@ -445,20 +476,11 @@ __global__ void __launch_bounds__(256, 3) sirt_persistent_kernel(SirtParams p) {
         }
         const int ph2 = ph + 1;
         if (p.dynamic && blockIdx.x == 0 && threadIdx.x == 0) p.work[(ph2 + 1) % 3] = 0u;
-        bp_phase(p, it, p.work + ph2 % 3, sh);
+        bp_phase<false>(p, it, p.work + ph2 % 3, sh);
         if (!grid_barrier(p.bar, nb, p.status, p.timeout_ns, &sh.flag)) return;
     }
 }
 
-// Programmatic dependent launch: a phase kernel launched with programmatic
-// stream serialization lets the next one be scheduled once all of its blocks
-// have started (launch_dependents), and the next one's blocks wait in
-// griddepcontrol.wait until this grid has completed and its writes are
-// visible.  Every block waits before it reads anything an earlier kernel
-// wrote, and before it exits, so completion stays transitive along the chain.
-// Launched without the attribute both instructions return at once.
-__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // Phase-split engine: the same two phases as ordinary launches, one per phase
 // and iteration.  The kernel boundary replaces the grid barrier, which for
@@ -468,8 +490,8 @@ __device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.l
 __global__ void __launch_bounds__(256, 5) sirt_fp_phase_kernel(SirtParams p, int it) {
     __shared__ SirtShared sh;
     chain_release();
-    chain_wait();
-    fp_phase(p, it, nullptr, sh);
+    fp_phase<true>(p, it, nullptr, sh);
+    chain_wait();                        // blocks without items wait too
 }
 
 // Forward phase of the split engine for a single problem (a stack of slices):
@@ -555,8 +577,8 @@ __global__ void __launch_bounds__(256) sirt_fp_stack_exact_kernel(SirtProblem q,
 __global__ void __launch_bounds__(256, 4) sirt_bp_phase_kernel(SirtParams p, int it, int *active) {
     __shared__ SirtShared sh;
     chain_release();
-    chain_wait();
     if (blockIdx.x == 0) {
+        chain_wait();                    // the stopping rule reads the forward phase's residuals
         if (threadIdx.x == 0) sh.any = 0;
         __syncthreads();
         int cnt = 0;
@@ -571,7 +593,8 @@ __global__ void __launch_bounds__(256, 4) sirt_bp_phase_kernel(SirtParams p, int
         __syncthreads();
         if (threadIdx.x == 0) *active = sh.any;
     }
-    bp_phase(p, it, nullptr, sh);
+    bp_phase<true>(p, it, nullptr, sh);
+    chain_wait();                        // blocks without items wait too
 }
 
 // Backward phase of the split engine for one large problem (a slice stack)
