@@ -424,7 +424,7 @@ int sirt_batch(synk_context *ctx, int nprob, const synk_sirt_problem *in, double
         const long long bp_tasks = (long long)q.nslices * ((q.size + 3) / 4) * ((q.size + 31) / 32);
         const long long fp_share = nprob > 1 ? fp_warps / nprob + 1 : fp_warps;
         const long long bp_share = nprob > 1 ? bp_warps / nprob + 1 : bp_warps;
-        h.bp_inrange = bp_windows_in_range(h.P, 32) ? 1 : 0;   // BP tiles of 4*(8/bp_split) <= 32 rows
+        h.bp_inrange = bp_windows_in_range(h.P, 32) ? 1 : 0;   // BP tiles of bp_pix*(8/bp_split) <= 32 rows
         h.fp_split = q.fp_split ? q.fp_split : pick_fp_split(fp_tasks, fp_share, q.size);
         h.bp_split = q.bp_split ? q.bp_split : pick_bp_split(bp_tasks, bp_share, q.a);
         // The phase kernels' items are blocks of 8 warps.  Measured with the
