@@ -23,10 +23,12 @@
 namespace synk {
 
 // Angles per staged chunk (and per partial sum before the compensated
-// total).  128 rather than 64: half the staging barriers, the whole angle set
-// of N=128 problems in one chunk (SIRT at N=128, 200 iterations: 4.08 -> 3.96
-// ms; dense backprojection 4.09 -> 4.07 ms).
-constexpr int kBpChunk = 128;
+// total).  Fewer chunks mean fewer staging barriers; the whole angle set of a
+// problem of up to 256 angles is one chunk.  SIRT at N=128 / 128 angles, 200
+// iterations: 4.08 ms with 64, 3.96 with 128; N=256 / 180 angles: 8.73 ms with
+// 128, 8.53 with 256; dense backprojection 4.09 / 4.07 / 4.05 ms with 64 /
+// 128 / 256.
+constexpr int kBpChunk = 256;
 
 struct BpStage {
     float4 cs[kBpChunk];   // cos, sin, h/b, 1/b
